@@ -1,0 +1,523 @@
+#!/usr/bin/env python3
+"""Benchmark of the Indigo2 hot path on one GB300 (or N replicas).
+
+Workload (one "step"): the six algorithms on the synthetic RMAT scale-22 graph
+(4,194,304 vertices, edge factor 16, a/b/c/d = .57/.19/.19/.05, seed 7, vertex
+ids permuted, self loops and duplicates removed, symmetrised, int32 weights in
+[1, 1000]): BFS and SSSP from each of 16 sources, CC, MIS, PageRank (FP32,
+d = 0.85, L1 residual 1e-6, <= 100 iterations) and triangle counting on the
+degree-ordered copy of the graph.
+
+Metric: GTEPS over the step, the reference's definition (g.edges / runtime,
+include/sssp_vertex_cuda.h:167) summed over the step's 36 runs:
+value = 36 * E / step time.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+`--impl ours` (default) prints one JSON line with the device-resident value,
+the end-to-end value through the reference-facing C ABI with host buffers,
+the roofline of the dominant kernel and the CPU baseline.  `--impl reference`
+times the reference's CPU algorithms (the oracle's threaded restatement of the
+best published C++ variants) on the host cores for the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT / "parallelization-artifact-sc23_gb300"))
+sys.path.insert(0, str(ROOT))
+
+SCALE, EDGE_FACTOR, RMAT_ABC, SEED, MAXW = 22, 16, (0.57, 0.19, 0.19), 7, 1000
+N_SOURCES = 16
+PR_EPS, PR_MAX_ITER = 1e-6, 100
+RUNS_PER_STEP = 2 * N_SOURCES + 4
+METRIC = "GTEPS (RMAT-22: 16x BFS + 16x SSSP + CC + MIS + PR + TC)"
+UNIT = "GTEPS"
+ALGOS = ["bfs", "sssp", "cc", "mis", "pr", "tc"]
+LAUNCHES_PER_CALL = {"bfs": 1, "sssp": 1, "cc": 4, "mis": 1, "pr": 1, "tc": 3}  # dominant-kernel launches
+
+
+def log(*a):
+    print(*a, file=sys.stderr, flush=True)
+
+
+# ----------------------------------------------------------------------------- dist
+class Dist:
+    def __init__(self):
+        self.world = int(os.environ.get("WORLD_SIZE", "1"))
+        self.rank = int(os.environ.get("RANK", "0"))
+        self.local = int(os.environ.get("LOCAL_RANK", "0"))
+        self.pg = None
+        if self.world > 1:
+            import torch.distributed as td
+            td.init_process_group("gloo")
+            self.td = td
+
+    def barrier(self):
+        if self.world > 1:
+            self.td.barrier()
+
+    def max(self, x: float) -> float:
+        if self.world == 1:
+            return x
+        import torch
+        t = torch.tensor([x], dtype=torch.float64)
+        self.td.all_reduce(t, op=self.td.ReduceOp.MAX)
+        return float(t.item())
+
+    def close(self):
+        if self.world > 1:
+            self.td.destroy_process_group()
+
+
+# ----------------------------------------------------------------------------- graph
+def make_workload(ig):
+    t0 = time.time()
+    g = ig.rmat(SCALE, EDGE_FACTOR, *RMAT_ABC, seed=SEED, maxw=MAXW, permute=True)
+    gd = g.degree_ordered()
+    sources = g.pick_sources(N_SOURCES, seed=SEED)
+    log(f"[bench] RMAT-{SCALE}: V={g.nodes} E={g.edges} generated in {time.time() - t0:.1f}s")
+    return g, gd, sources
+
+
+def algorithmic_bytes(g, gd, pr_iters: int) -> dict:
+    """Bytes each algorithm must move once (4-byte words, each logical access
+    counted once): BFS 4(V+1)+8E+4V, SSSP 12E+8V, CC 8E+8V, MIS 8E+12V,
+    PR iters*(8E+20V), TC sum over oriented edges u->v of 4(d+(u)+d+(v)) + 4E + 4V."""
+    V, E = g.nodes, g.edges
+    deg = gd.degree().astype(np.int64)
+    # degree-ordered ids: the oriented out-degree is the count of neighbours with a larger id
+    src = np.repeat(np.arange(gd.nodes, dtype=np.int64), deg)
+    up = gd.nlist.astype(np.int64) > src
+    dplus = np.bincount(src[up], minlength=gd.nodes).astype(np.int64)
+    tc = 4 * int((dplus[src[up]] + dplus[gd.nlist[up]]).sum()) + 4 * E + 4 * V
+    return {
+        "bfs": 4 * (V + 1) + 8 * E + 4 * V,
+        "sssp": 12 * E + 8 * V,
+        "cc": 8 * E + 8 * V,
+        "mis": 8 * E + 12 * V,
+        "pr": max(1, pr_iters) * (8 * E + 20 * V),
+        "tc": tc,
+    }
+
+
+# ----------------------------------------------------------------------------- clocks
+class ClockSampler:
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.file = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        self.proc = None
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(gpu_index), f"--query-gpu={self.QUERY}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=self.file, stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.file.flush()
+        self.file.seek(0)
+        rows = [r.split(",") for r in self.file.read().strip().splitlines() if r.count(",") >= 8]
+        os.unlink(self.file.name)
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            try:
+                sm.append(float(r[1]))
+                mx.append(float(r[2]))
+            except ValueError:
+                continue
+            for nm, val in zip(names, r[5:9]):
+                if val.strip().lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ----------------------------------------------------------------------------- ours
+def run_ours(args, dist: Dist):
+    import indigo_gb300 as ig
+
+    ig.check(ig.load().ig_set_device(dist.local))
+    g, gd, sources = make_workload(ig)
+    V, E = g.nodes, g.edges
+
+    d = ig.DeviceCSR(g)
+    dd = ig.DeviceCSR(gd)
+    stream = ig.create_stream()
+    G = ig.DeviceGraph(d)
+    GT = ig.DeviceGraph(dd)
+    G.set_stream(stream)
+    GT.set_stream(stream)
+    dist_buf = ig.DeviceBuffer(4 * V)
+    lab = ig.DeviceBuffer(4 * V)
+    st = ig.DeviceBuffer(4 * V)
+    init = np.full(V, np.float32(1.0) / np.float32(V), np.float32)
+    scores0 = ig.DeviceBuffer.from_array(init)
+    scores = ig.DeviceBuffer(4 * V)
+    count = ig.DeviceBuffer(8)
+    L = ig.load()
+    ev = {k: (ig.Event(), ig.Event()) for k in ALGOS}
+    acc = {k: 0.0 for k in ALGOS}
+
+    def step(timed: bool):
+        ev["bfs"][0].record(stream)
+        for s in sources:
+            G.bfs(int(s), dist_buf)
+        ev["bfs"][1].record(stream)
+        ev["sssp"][0].record(stream)
+        for s in sources:
+            G.sssp(int(s), dist_buf)
+        ev["sssp"][1].record(stream)
+        ev["cc"][0].record(stream)
+        G.cc(lab)
+        ev["cc"][1].record(stream)
+        ev["mis"][0].record(stream)
+        G.mis(st)
+        ev["mis"][1].record(stream)
+        ev["pr"][0].record(stream)
+        ig.check(L.ig_memcpy_async(scores.ptr, scores0.ptr, 4 * V, 3, stream))
+        G.pagerank(scores, PR_EPS, PR_MAX_ITER)
+        ev["pr"][1].record(stream)
+        ev["tc"][0].record(stream)
+        GT.tc(count)
+        ev["tc"][1].record(stream)
+        if timed:
+            for k in ALGOS:
+                acc[k] += ev[k][0].elapsed_ms(ev[k][1])
+
+    # warm-up (untimed), then validate the outputs of one step
+    for _ in range(args.warmup):
+        step(False)
+    G.synchronize()
+    info_g, info_t = G.last_run(), GT.last_run()
+    if info_g.status or info_t.status:
+        raise RuntimeError(f"device run failed: status {info_g.status} / {info_t.status}")
+    pr_iters = info_g.iterations
+    validation = validate(ig, g, G, GT, sources, dist_buf, lab, st, scores, count)
+
+    t_start, t_end = ig.Event(), ig.Event()
+    launches0 = ig.kernel_launches()
+    clocks = ClockSampler(dist.local)
+    dist.barrier()
+    ig.check(L.ig_stream_synchronize(stream))
+    t_start.record(stream)
+    for _ in range(args.steps):
+        step(True)
+    t_end.record(stream)
+    ig.check(L.ig_stream_synchronize(stream))
+    dist.barrier()
+    clk = clocks.stop()
+    ms_total = t_start.elapsed_ms(t_end)
+    launches = ig.kernel_launches() - launches0
+    if G.last_run().status or GT.last_run().status:
+        raise RuntimeError("device error during the timed steps")
+    ms_max = dist.max(ms_total)
+    ms_per_step = ms_max / args.steps
+    value = dist.world * RUNS_PER_STEP * E / (ms_per_step * 1e-3) / 1e9
+
+    # per-algorithm numbers and the roofline of the dominant kernel
+    peaks = load_peaks()
+    abytes = algorithmic_bytes(g, gd, pr_iters)
+    calls = {"bfs": N_SOURCES, "sssp": N_SOURCES, "cc": 1, "mis": 1, "pr": 1, "tc": 1}
+    per = {}
+    for k in ALGOS:
+        ms_call = acc[k] / args.steps / calls[k]
+        gbs = abytes[k] / (ms_call * 1e-3) / 1e9
+        per[k] = {"ms_per_call": round(ms_call, 4), "gteps": round(E / (ms_call * 1e-3) / 1e9, 3),
+                  "algorithmic_bytes": abytes[k], "achieved_gbs": round(gbs, 1),
+                  "hbm_frac": round(gbs / peaks["hbm_gbs"], 4)}
+    per["pr"]["iterations"] = pr_iters
+    shares = {k: acc[k] / max(1e-9, sum(acc.values())) for k in ALGOS}
+    dom = max(shares, key=shares.get)
+    traffic = load_traffic().get(dom)
+    roofline = {"bound": "hbm", "kernel": dom, "achieved": per[dom]["achieved_gbs"], "peak": peaks["hbm_gbs"],
+                "peak_source": peaks["source"], "unit": "GB/s",
+                "frac": round(per[dom]["achieved_gbs"] / peaks["hbm_gbs"], 4), "traffic": traffic,
+                "algorithmic_bytes_per_launch": abytes[dom], "share_of_step": round(shares[dom], 4),
+                "timing": "CUDA events around each call on the launching stream, averaged over the timed steps"}
+
+    e2e = None
+    if not args.no_e2e:
+        e2e = run_e2e(ig, g, gd, sources, args, dist)
+
+    cpu = None
+    if dist.world == 1 and not args.no_cpu_baseline:
+        cpu = cpu_baseline(g, gd, sources, validation)
+
+    for h in (G, GT):
+        h.close()
+    d.close()
+    dd.close()
+    out = {
+        "metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": dist.world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(ms_per_step, 3), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "int32/f32", "data": "synthetic",
+        "config": {"workload": f"rmat{SCALE}_ef{EDGE_FACTOR}_six_algorithms", "vertices": V, "edges": E,
+                   "rmat_abcd": [0.57, 0.19, 0.19, 0.05], "seed": SEED, "weights": f"[1,{MAXW}]",
+                   "sources": N_SOURCES, "pr_epsilon": PR_EPS, "pr_max_iter": PR_MAX_ITER,
+                   "tc_input": "degree-ordered relabelling", "runs_per_step": RUNS_PER_STEP,
+                   "l2": "inputs larger than L2 (nlist+eweight %.0f MB > 129 MB)" % (8 * E / 1e6),
+                   "parallelism": "replicas" if dist.world > 1 else "single GPU"},
+        "e2e": e2e, "roofline": roofline, "cpu_baseline": cpu, "clocks": clk, "gpu_launches": launches,
+        "per_algo": per, "validation": validation,
+    }
+    return out
+
+
+def run_e2e(ig, g, gd, sources, args, dist: Dist):
+    """Same step through the drop-in C ABI (reference pointer residency) with
+    the graph copied from pinned host memory every step and every result read
+    back to pinned host memory."""
+    import ctypes
+    L = ig.load()
+    V, E = g.nodes, g.edges
+
+    def pinned(nbytes):
+        p = ctypes.c_void_p()
+        ig.check(L.ig_host_alloc_pinned(ctypes.byref(p), max(1, nbytes)))
+        return p.value
+
+    def pinned_copy(a: np.ndarray):
+        p = pinned(a.nbytes)
+        ctypes.memmove(p, a.ctypes.data, a.nbytes)
+        return p
+
+    hp = {"ni": pinned_copy(g.nindex), "nl": pinned_copy(g.nlist), "ew": pinned_copy(g.eweight),
+          "dni": pinned_copy(gd.nindex), "dnl": pinned_copy(gd.nlist), "deg": pinned_copy(g.degree())}
+    init = np.full(V, np.float32(1.0) / np.float32(V), np.float32)
+    h_scores = pinned(4 * V)
+    h_out = pinned(4 * V)
+    d = ig.DeviceCSR(g)    # device arrays reused; refilled from pinned memory each step
+    dd = ig.DeviceCSR(gd)
+    hc = ig.CSR()
+    hc.nodes, hc.edges = V, E
+    ip = ctypes.POINTER(ctypes.c_int)
+    hc.nindex, hc.nlist, hc.eweight = ctypes.cast(hp["ni"], ip), ctypes.cast(hp["nl"], ip), ip()
+    t = ctypes.c_double()
+    cnt = ctypes.c_longlong()
+    it = ctypes.c_int()
+    h2d = 4 * (V + 1) + 8 * E + 4 * (V + 1) + 4 * E
+    d2h = 4 * V * (2 * N_SOURCES + 2) + 8 + 4 * V
+    h2d += 4 * (V + 1) + 4 * E + 4 * V + 4 * V  # PR_GPU uploads nindex, nlist, degree, scores itself
+
+    def step():
+        ig.check(L.ig_memcpy(ctypes.cast(d.c.nindex, ctypes.c_void_p), hp["ni"], 4 * (V + 1), 1))
+        ig.check(L.ig_memcpy(ctypes.cast(d.c.nlist, ctypes.c_void_p), hp["nl"], 4 * E, 1))
+        ig.check(L.ig_memcpy(ctypes.cast(d.c.eweight, ctypes.c_void_p), hp["ew"], 4 * E, 1))
+        ig.check(L.ig_memcpy(ctypes.cast(dd.c.nindex, ctypes.c_void_p), hp["dni"], 4 * (V + 1), 1))
+        ig.check(L.ig_memcpy(ctypes.cast(dd.c.nlist, ctypes.c_void_p), hp["dnl"], 4 * E, 1))
+        for s in sources:
+            ig.check(L.ig_bfs_vertex(int(s), ctypes.byref(d.c), h_out, ctypes.byref(t)))
+        for s in sources:
+            ig.check(L.ig_sssp_vertex(int(s), ctypes.byref(d.c), h_out, ctypes.byref(t)))
+        ig.check(L.ig_cc_vertex(ctypes.byref(d.c), h_out, ctypes.byref(t)))
+        ig.check(L.ig_mis_vertex(ctypes.byref(d.c), None, h_out, ctypes.byref(t)))
+        ctypes.memmove(h_scores, init.ctypes.data, 4 * V)
+        ig.check(L.ig_pr(ctypes.byref(hc), h_scores, hp["deg"], PR_EPS, PR_MAX_ITER, ctypes.byref(it),
+                         ctypes.byref(t)))
+        ig.check(L.ig_tc_vertex(ctypes.byref(cnt), V, ctypes.cast(dd.c.nindex, ctypes.c_void_p),
+                                ctypes.cast(dd.c.nlist, ctypes.c_void_p), ctypes.byref(t)))
+
+    for _ in range(max(1, args.warmup)):
+        step()
+    ig.check(L.ig_device_synchronize())
+    dist.barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        step()
+    ig.check(L.ig_device_synchronize())
+    el = time.perf_counter() - t0
+    el = dist.max(el)
+    d.close()
+    dd.close()
+    for p in list(hp.values()) + [h_scores, h_out]:
+        L.ig_host_free_pinned(p)
+    value = dist.world * RUNS_PER_STEP * E * args.steps / el / 1e9
+    return {"value": round(value, 3), "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+            "ms_per_step": round(1e3 * el / args.steps, 3),
+            "api": "drop-in C ABI (ig_bfs_vertex ... ig_tc_vertex), host wall clock, pinned host buffers"}
+
+
+def validate(ig, g, G, GT, sources, dist_buf, lab, st, scores, count) -> dict:
+    """Size-independent properties of one step's results (numpy, untimed)."""
+    V = g.nodes
+    src = np.repeat(np.arange(V, dtype=np.int64), g.degree())
+    nl = g.nlist.astype(np.int64)
+    INF = 2147483647
+    s0 = int(sources[0])
+    G.bfs(s0, dist_buf)
+    dd = dist_buf.to_array(np.int32, V).astype(np.int64)
+    reach = dd < INF
+    ok_bfs = dd[s0] == 0 and bool(np.all(np.abs(dd[src] - dd[nl])[reach[src]] <= 1)) and \
+        bool(np.all(reach[src] == reach[nl]))
+    G.sssp(s0, dist_buf)
+    ds = dist_buf.to_array(np.int32, V).astype(np.int64)
+    w = g.eweight.astype(np.int64)
+    r = ds[src] < INF
+    ok_sssp = ds[s0] == 0 and bool(np.all(ds[nl][r] <= ds[src][r] + w[r]))
+    # tightness: every reached vertex but the source has a neighbour on a shortest path
+    tight = np.zeros(V, bool)
+    hit = r & (ds[nl] == ds[src] + w)
+    tight[nl[hit]] = True
+    tight[s0] = True
+    ok_sssp = ok_sssp and bool(np.all(tight[ds < INF]))
+    G.cc(lab)
+    lb = lab.to_array(np.int32, V).astype(np.int64)
+    ok_cc = bool(np.all(lb[src] == lb[nl])) and bool(np.all(lb <= np.arange(V))) and bool(np.all(lb[lb] == lb))
+    G.mis(st)
+    ms = st.to_array(np.int32, V)
+    x = np.arange(V, dtype=np.uint64) + np.uint64(712313887)
+    x &= np.uint64(0xFFFFFFFF)
+    for _ in range(2):
+        x = (((x >> np.uint64(16)) ^ x) * np.uint64(0x45D9F3B)) & np.uint64(0xFFFFFFFF)
+    pr = ((x >> np.uint64(16)) ^ x).astype(np.int64)
+    key = pr * (1 << 32) + np.arange(V, dtype=np.int64)  # (priority, id) order
+    inset = ms == 1
+    larger = key[nl] > key[src]
+    blocked = np.zeros(V, bool)
+    blocked[src[larger & inset[nl]]] = True  # has a larger neighbour in the set
+    ok_mis = bool(np.all(np.isin(ms, [1, 2]))) and bool(np.all(inset == ~blocked))
+    sc = scores.to_array(np.float32, V)
+    ok_pr = bool(np.all(np.isfinite(sc))) and 0.5 < float(sc.sum()) <= 1.0 + 1e-4
+    GT.tc(count)
+    tc = int(count.to_array(np.uint64, 1)[0])
+    G.synchronize()
+    return {"bfs_levels_consistent": ok_bfs, "sssp_triangle_and_tight": ok_sssp, "cc_min_label": ok_cc,
+            "mis_greedy_unique": ok_mis, "pr_mass": ok_pr, "tc_count": tc}
+
+
+# ----------------------------------------------------------------------------- peaks / traffic
+def load_peaks() -> dict:
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        m = json.loads(p.read_text())
+        return {"hbm_gbs": float(m["hbm_gbs"]), "source": "measured (MEASURED_PEAKS.json hbm_gbs, STREAM copy)"}
+    return {"hbm_gbs": 6800.0, "source": "fallback 6.8 TB/s"}
+
+
+def load_traffic() -> dict:
+    """Per-launch DRAM bytes (read + write) of each algorithm's dominant kernel
+    from the committed ncu summary profiles/ncu_traffic.txt, when present."""
+    p = ROOT / "profiles" / "ncu_traffic.txt"
+    out = {}
+    if p.exists():
+        for line in p.read_text().splitlines():
+            parts = line.split()
+            if len(parts) >= 2 and not line.startswith("#"):
+                try:
+                    out[parts[0]] = int(float(parts[1]))
+                except ValueError:
+                    pass
+    return out
+
+
+# ----------------------------------------------------------------------------- CPU
+def cpu_sample(g, gd, sources, threads):
+    """One bounded sample of the step on the host cores with the oracle's
+    threaded restatement of the best published C++ variants: BFS and SSSP from
+    one source (scaled x16), CC, MIS, PR (eps 1e-6), TC on the degree-ordered graph."""
+    from oracle import oracle as orc
+    s = int(sources[0])
+    t = {}
+    _, t["bfs"] = orc.bfs_threads(g, s, threads)
+    _, t["sssp"] = orc.sssp_threads(g, s, threads)
+    _, t["cc"] = orc.cc_threads(g, threads)
+    _, t["mis"] = orc.mis_threads(g, threads)
+    _, it, t["pr"] = orc.pr_threads(g, threads, PR_EPS, PR_MAX_ITER)
+    tc, t["tc"] = orc.tc_threads(gd, threads)
+    step_s = N_SOURCES * (t["bfs"] + t["sssp"]) + t["cc"] + t["mis"] + t["pr"] + t["tc"]
+    return step_s, t, tc, it
+
+
+def cpu_baseline(g, gd, sources, validation):
+    threads = os.cpu_count() or 1
+    t0 = time.time()
+    step_s, t, tc, it = cpu_sample(g, gd, sources, threads)
+    value = RUNS_PER_STEP * g.edges / step_s / 1e9
+    validation["tc_matches_cpu"] = (tc == validation.get("tc_count"))
+    return {"value": round(value, 4), "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": "one pass of the step with BFS/SSSP from 1 of the 16 sources (x16 in the step time), "
+                      "CC, MIS, PR (%d iterations), TC; oracle/indigo_oracle.c threaded restatement of the "
+                      "best published C++ variants, %.1fs wall" % (it, time.time() - t0),
+            "seconds": {k: round(v, 4) for k, v in t.items()}}
+
+
+def run_reference(args, dist: Dist):
+    import indigo_gb300 as ig  # host-side generators only (no GPU use)
+    g, gd, sources = make_workload(ig)
+    threads = os.cpu_count() or 1
+    for _ in range(args.warmup):
+        cpu_sample(g, gd, sources, threads)
+    total = 0.0
+    detail = None
+    for _ in range(args.steps):
+        step_s, t, tc, it = cpu_sample(g, gd, sources, threads)
+        total += step_s
+        detail = t
+    ms_per_step = 1e3 * total / args.steps
+    value = RUNS_PER_STEP * g.edges / (total / args.steps) / 1e9
+    sample = ("each step: BFS/SSSP from 1 of the 16 sources (x16 in the step time), CC, MIS, PR, TC on the "
+              "degree-ordered graph; threaded restatement of the best published C++ variants "
+              "(oracle/indigo_oracle.c; the reference's own programs are built for this container's "
+              "architecture only)")
+    return {"impl": "reference", "metric": METRIC, "value": round(value, 4), "unit": UNIT, "n_gpus": dist.world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms_per_step, 3),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32/f32",
+            "data": "synthetic",
+            "config": {"workload": f"rmat{SCALE}_ef{EDGE_FACTOR}_six_algorithms", "vertices": g.nodes,
+                       "edges": g.edges, "sources": N_SOURCES, "pr_epsilon": PR_EPS},
+            "cpu_baseline": {"value": round(value, 4), "unit": UNIT, "cores": threads, "kind": "port",
+                             "sample": sample, "seconds": {k: round(v, 4) for k, v in detail.items()}},
+            "e2e": {"value": round(value, 4), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        log("[bench] warm-up raised to 3 (minimum)")
+        args.warmup = 3
+    dist = Dist()
+    try:
+        if args.impl == "reference":
+            if dist.rank != 0:
+                return
+            out = run_reference(args, dist)
+        else:
+            out = run_ours(args, dist)
+        if dist.rank == 0:
+            print(json.dumps(out), flush=True)
+    finally:
+        dist.close()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,168 @@
+// Breadth-first search: one persistent, cooperatively launched kernel per
+// call.  Replaces the per-level host loop of the reference CUDA variants
+// (e.g. codes/cuda/bfs-cuda/BFS_CUDA_V_Topo_Push_Determ_IntType_ReadWrite_
+// NonPersist_Atomic_Thread_NoBoundsBug2_NoBoundsBug1.cu:56-108, one launch
+// plus a 4-byte device-to-host copy per level) by grid barriers on the device.
+//
+// Output semantics follow include/bfs_vertex_cuda.h: dist[v] = number of
+// edges on a shortest path from src, INT_MAX (`maxval`, :46) if unreachable.
+//
+// Each level is either
+//   top-down : the frontier queue is expanded 32 vertices per warp with the
+//              load-balanced warp expansion; a vertex is claimed with one
+//              atomicCAS on dist (INT_MAX -> level+1) and appended to the next
+//              queue with one atomic per warp (the worklist idiom of the
+//              reference's *_Data_*_NonDup variants, warp-aggregated);
+//              vertices above the hub degree are expanded by the whole grid;
+//   bottom-up: every unvisited vertex scans its neighbours for one at the
+//              current level and stops at the first (Beamer's direction
+//              optimisation; the graph is symmetric as in the reference).
+// The direction is chosen from the frontier's edge count and vertex count,
+// identically in every block after the level's barrier.
+#include "ig_device.cuh"
+#include "ig_options.h"
+
+namespace {
+
+constexpr int kThreads = 256;
+
+struct BfsArgs {
+  const int* __restrict__ nindex;
+  const int* __restrict__ nlist;
+  int nodes;
+  long long edges;
+  int src;
+  int* dist;
+  int* qa;
+  int* qb;
+  int* hubs;
+  IgCtl* ctl;
+  unsigned long long timeout_ns;
+  int hub_degree;
+  int alpha;
+  int beta;
+};
+
+// ctl->i32[s] : size of the queue built during a level with slot s (= level % 3)
+// ctl->i32[3 + s]: hub count, ctl->u64[s]: sum of degrees of the queued vertices
+
+__global__ void __launch_bounds__(kThreads) bfs_persistent(BfsArgs a) {
+  using namespace ig;
+  IgCtl* ctl = a.ctl;
+  const int lane = lane_id();
+  const long long gtid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long long gthreads = (long long)gridDim.x * blockDim.x;
+  const int warp_g = (int)(gtid >> 5);
+  const int nwarps = (int)(gthreads >> 5);
+
+  for (long long v = gtid; v < a.nodes; v += gthreads) a.dist[v] = (v == a.src) ? 0 : kInf;
+  if (gtid == 0) a.qa[0] = a.src;
+  if (!grid_sync(ctl, a.timeout_ns)) return;
+
+  int* cur = a.qa;
+  int* nxt = a.qb;
+  int cur_size = 1;
+  bool bottom_up = false;
+  const long long src_deg = __ldg(&a.nindex[a.src + 1]) - __ldg(&a.nindex[a.src]);
+  long long unexplored = a.edges - src_deg;
+  int level = 0;
+
+  while (cur_size > 0) {
+    const int slot = level % 3;
+    if (gtid == 0) {
+      const int ns = (level + 1) % 3;
+      ctl->i32[ns] = 0;
+      ctl->i32[3 + ns] = 0;
+      ctl->u64[ns] = 0;
+    }
+    int* qsize = &ctl->i32[slot];
+    int* nhub = &ctl->i32[3 + slot];
+    unsigned long long* fedges = &ctl->u64[slot];
+    const int next_level = level + 1;
+
+    if (!bottom_up) {
+      auto visit = [&](bool act, int e, int) {
+        bool claim = false;
+        int w = 0;
+        long long wdeg = 0;
+        if (act) {
+          w = __ldg(&a.nlist[e]);
+          if (a.dist[w] == kInf && atomicCAS(&a.dist[w], kInf, next_level) == kInf) {
+            claim = true;
+            wdeg = __ldg(&a.nindex[w + 1]) - __ldg(&a.nindex[w]);
+          }
+        }
+        warp_append_w(claim, w, wdeg, nxt, qsize, fedges, a.nodes, ctl);
+      };
+      for (int base = warp_g * 32; base < cur_size; base += nwarps * 32) {
+        const int i = base + lane;
+        int v = 0, beg = 0, deg = 0;
+        if (i < cur_size) {
+          v = cur[i];
+          beg = __ldg(&a.nindex[v]);
+          deg = __ldg(&a.nindex[v + 1]) - beg;
+        }
+        const bool hub = deg > a.hub_degree;
+        warp_append(hub, v, a.hubs, nhub, a.nodes, ctl);
+        warp_expand(beg, hub ? 0 : deg, visit);
+      }
+      if (!grid_sync(ctl, a.timeout_ns)) return;
+      const int nh = ld_relaxed(nhub);
+      if (nh > 0) {
+        grid_expand_hubs(a.nindex, a.hubs, nh, [&](bool act, int e, int) { visit(act, e, 0); });
+        if (!grid_sync(ctl, a.timeout_ns)) return;
+      }
+    } else {
+      for (long long base = gtid & ~31LL; base < a.nodes; base += gthreads) {
+        const long long v = base + lane;
+        bool found = false;
+        long long deg = 0;
+        if (v < a.nodes && a.dist[v] == kInf) {
+          const int b = __ldg(&a.nindex[v]), e = __ldg(&a.nindex[v + 1]);
+          deg = e - b;
+          for (int k = b; k < e; k++) {
+            if (a.dist[__ldg(&a.nlist[k])] == level) {
+              found = true;
+              break;
+            }
+          }
+          if (found) a.dist[v] = next_level;
+        }
+        warp_append_w(found, (int)v, deg, nxt, qsize, fedges, a.nodes, ctl);
+      }
+      if (!grid_sync(ctl, a.timeout_ns)) return;
+    }
+
+    const int nf = ld_relaxed(qsize);
+    const long long mf = (long long)ld_relaxed(fedges);
+    unexplored -= mf;
+    level = next_level;
+    if (!bottom_up) {
+      if (mf > unexplored / a.alpha) bottom_up = true;
+    } else {
+      if ((long long)nf * a.beta < a.nodes) bottom_up = false;
+    }
+    cur_size = nf;
+    int* t = cur;
+    cur = nxt;
+    nxt = t;
+  }
+  if (gtid == 0) ctl->iterations = level;
+}
+
+}  // namespace
+
+int igk_bfs(IgExec* ex, const ig_csr* dg, int src, int* d_dist) {
+  const size_t vb = (size_t)dg->nodes * sizeof(int);
+  void *qa, *qb, *hubs;
+  int rc;
+  if ((rc = ig_scratch_get(ex->scratch, IG_SLOT_Q0, vb, &qa))) return rc;
+  if ((rc = ig_scratch_get(ex->scratch, IG_SLOT_Q1, vb, &qb))) return rc;
+  if ((rc = ig_scratch_get(ex->scratch, IG_SLOT_Q2, vb, &hubs))) return rc;
+  if ((rc = ig_exec_reset(ex))) return rc;
+  const IgOptions& o = ig_options();
+  BfsArgs a{dg->nindex, dg->nlist, dg->nodes, dg->edges, src, d_dist, (int*)qa, (int*)qb, (int*)hubs,
+            ex->d_ctl, ex->timeout_ns, o.hub_degree, o.bfs_alpha, o.bfs_beta};
+  void* args[] = {&a};
+  return ig_launch_coop(ex, (const void*)bfs_persistent, kThreads, 0, o.blocks_per_sm, args, nullptr);
+}

@@ -1,0 +1,142 @@
+// Connected components by union-find hooking and pointer jumping.
+//
+// The reference computes labels by min-label propagation until no label
+// changes (codes/cpp/cc-cpp/CC_CPP_V_Topo_Push_IntType_ReadModifyWrite_Determ_
+// NoBoundsBug_Block_Atomic.cpp; CUDA: codes/cuda/cc-cuda/CC_CUDA_V_Topo_Push_
+// Determ_IntType_ReadModifyWrite_NonPersist_CudaAtomic_Thread_NoBoundsBug2_
+// NoBoundsBug1.cu:57-77), whose fixed point is label[v] = the smallest vertex
+// id in v's component; rounds grow with the graph diameter.  Here every
+// undirected edge is visited once and the two trees are linked by always
+// hooking the larger root under the smaller one with atomicCAS, so a root is
+// the minimum of its tree; a final pass points every vertex at its root.
+// The result is the same min-id labelling in a number of passes independent
+// of the diameter.
+//
+//   init   : parent[v] = min(v, first neighbour)   (adjacency is sorted)
+//   hook   : for each edge (u, v) with v < u: union(u, v); vertices above the
+//            hub degree are deferred to an edge-balanced grid-wide pass
+//   compress: label[v] = root(v)
+#include "ig_device.cuh"
+#include "ig_options.h"
+
+namespace {
+
+constexpr int kThreads = 256;
+
+__device__ __forceinline__ int load_parent(const int* parent, int x) {
+  return *((const volatile int*)parent + x);
+}
+
+// Root of x with path halving (writes only ever point a vertex at one of its
+// ancestors, so they are safe under concurrent hooking).
+__device__ __forceinline__ int find_root(int* parent, int x) {
+  while (true) {
+    const int p = load_parent(parent, x);
+    if (p == x) return x;
+    const int gp = load_parent(parent, p);
+    if (gp == p) return p;
+    parent[x] = gp;
+    x = gp;
+  }
+}
+
+__device__ __forceinline__ void unite(int* parent, int u, int v) {
+  int ru = find_root(parent, u);
+  int rv = find_root(parent, v);
+  while (ru != rv) {
+    if (ru < rv) {
+      const int t = ru;
+      ru = rv;
+      rv = t;
+    }
+    // ru > rv: hook the larger root under the smaller
+    const int old = atomicCAS(&parent[ru], ru, rv);
+    if (old == ru) return;
+    ru = find_root(parent, old);
+    rv = find_root(parent, rv);
+  }
+}
+
+__global__ void cc_init(const int* __restrict__ nindex, const int* __restrict__ nlist, int n, int* parent) {
+  for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < n; v += gridDim.x * blockDim.x) {
+    const int b = __ldg(&nindex[v]), e = __ldg(&nindex[v + 1]);
+    int p = v;
+    if (b < e) {
+      const int m = __ldg(&nlist[b]);
+      if (m < v) p = m;
+    }
+    parent[v] = p;
+  }
+}
+
+__global__ void __launch_bounds__(kThreads) cc_hook(const int* __restrict__ nindex, const int* __restrict__ nlist,
+                                                    int n, int* parent, int* hubs, IgCtl* ctl, int hub_degree) {
+  using namespace ig;
+  const int lane = lane_id();
+  const long long gtid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long long gthreads = (long long)gridDim.x * blockDim.x;
+  for (long long base = gtid & ~31LL; base < n; base += gthreads) {
+    const long long v = base + lane;
+    int beg = 0, deg = 0;
+    if (v < n) {
+      beg = __ldg(&nindex[v]);
+      deg = __ldg(&nindex[v + 1]) - beg;
+    }
+    const bool hub = deg > hub_degree;
+    warp_append(hub, (int)v, hubs, &ctl->i32[0], n, ctl);
+    const int vv = (int)v;
+    warp_expand(beg, hub ? 0 : deg, [&](bool act, int e, int j) {
+      const int u = __shfl_sync(IG_FULL, vv, j);
+      if (act) {
+        const int w = __ldg(&nlist[e]);
+        if (w < u) unite(parent, u, w);
+      }
+    });
+  }
+}
+
+__global__ void __launch_bounds__(kThreads) cc_hook_hubs(const int* __restrict__ nindex,
+                                                         const int* __restrict__ nlist, int* parent,
+                                                         const int* hubs, const IgCtl* ctl) {
+  using namespace ig;
+  const int nh = ctl->i32[0];
+  if (nh == 0) return;
+  grid_expand_hubs(nindex, hubs, nh, [&](bool act, int e, int hv) {
+    if (act) {
+      const int w = __ldg(&nlist[e]);
+      if (w < hv) unite(parent, hv, w);
+    }
+  });
+}
+
+__global__ void cc_compress(int* parent, int n) {
+  for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < n; v += gridDim.x * blockDim.x) {
+    int r = parent[v];
+    while (true) {
+      const int p = parent[r];
+      if (p == r) break;
+      r = p;
+    }
+    parent[v] = r;
+  }
+}
+
+}  // namespace
+
+int igk_cc(IgExec* ex, const ig_csr* dg, int* d_label) {
+  const int n = dg->nodes;
+  void* hubs;
+  int rc;
+  if ((rc = ig_scratch_get(ex->scratch, IG_SLOT_Q2, (size_t)n * sizeof(int), &hubs))) return rc;
+  if ((rc = ig_exec_reset(ex))) return rc;
+  const IgOptions& o = ig_options();
+  const int grid_v = std::min((n + kThreads - 1) / kThreads, ex->sms * 16);
+  const int grid_w = std::max(1, std::min((n + kThreads - 1) / kThreads, ex->sms * 8));
+  cc_init<<<grid_v, kThreads, 0, ex->stream>>>(dg->nindex, dg->nlist, n, d_label);
+  cc_hook<<<grid_w, kThreads, 0, ex->stream>>>(dg->nindex, dg->nlist, n, d_label, (int*)hubs, ex->d_ctl,
+                                               o.hub_degree);
+  cc_hook_hubs<<<ex->sms * 4, kThreads, 0, ex->stream>>>(dg->nindex, dg->nlist, d_label, (int*)hubs, ex->d_ctl);
+  cc_compress<<<grid_v, kThreads, 0, ex->stream>>>(d_label, n);
+  ig_count_launches(4);
+  return ig_cuda_check((int)cudaGetLastError(), "cc launch");
+}

@@ -1,0 +1,347 @@
+// Device-side building blocks shared by the graph kernels:
+//   - relaxed / acquire / release accessors (hand-written PTX),
+//   - a grid barrier for cooperatively launched persistent kernels whose
+//     wait is bounded by %globaltimer and reports IG_ERR_TIMEOUT,
+//   - warp-aggregated queue append (one atomic per warp),
+//   - load-balanced expansion of the adjacency lists of 32 vertices held one
+//     per lane (the warp walks their concatenated edge ranges 32 at a time).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <climits>
+#include <cstdint>
+
+#include "ig_internal.h"
+
+#define IG_FULL 0xffffffffu
+
+namespace ig {
+
+constexpr int kInf = INT_MAX;
+
+__device__ __forceinline__ int lane_id() { return threadIdx.x & 31; }
+__device__ __forceinline__ unsigned lanemask_lt() {
+  unsigned m;
+  asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+  return m;
+}
+
+__device__ __forceinline__ unsigned long long globaltimer() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+__device__ __forceinline__ unsigned ld_acquire(const unsigned* p) {
+  unsigned v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ void st_release(unsigned* p, unsigned v) {
+  asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+__device__ __forceinline__ unsigned atom_add_acqrel(unsigned* p, unsigned v) {
+  unsigned old;
+  asm volatile("atom.acq_rel.gpu.global.add.u32 %0, [%1], %2;"
+               : "=r"(old)
+               : "l"(p), "r"(v)
+               : "memory");
+  return old;
+}
+__device__ __forceinline__ int ld_relaxed(const int* p) {
+  int v;
+  asm volatile("ld.relaxed.gpu.global.s32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ unsigned long long ld_relaxed(const unsigned long long* p) {
+  unsigned long long v;
+  asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ long long ld_relaxed(const long long* p) {
+  long long v;
+  asm volatile("ld.relaxed.gpu.global.s64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ double ld_relaxed(const double* p) {
+  double v;
+  asm volatile("ld.relaxed.gpu.global.f64 %0, [%1];" : "=d"(v) : "l"(p) : "memory");
+  return v;
+}
+
+// Records the first device-side error.
+__device__ __forceinline__ void raise(IgCtl* ctl, int code) { atomicCAS(&ctl->err, 0, code); }
+
+// Grid-wide barrier for a cooperative launch.  Returns false (in every
+// thread of the block) when the barrier failed: another block raised an
+// error, or the wait exceeded `timeout_ns`; the caller must then return.
+// Pattern: block barrier, one thread publishes its block's writes with a
+// gpu-scope fence and arrives; the last arriver resets the count and bumps
+// the generation with release semantics; the others spin on an acquire load
+// of the generation (bounded), then fence and release their block.
+__device__ __forceinline__ bool grid_sync(IgCtl* ctl, unsigned long long timeout_ns) {
+  __shared__ int s_ok;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int ok = 1;
+    IgSync* s = &ctl->sync;
+    const unsigned gen = ld_acquire(&s->gen);
+    __threadfence();
+    if (atom_add_acqrel(&s->arrive, 1u) == gridDim.x - 1) {
+      atomicExch(&s->arrive, 0u);
+      st_release(&s->gen, gen + 1);
+    } else {
+      const unsigned long long t0 = globaltimer();
+      unsigned spins = 0;
+      while (ld_acquire(&s->gen) == gen) {
+        if ((++spins & 63u) == 0) {
+          if (ld_relaxed(&ctl->err) != 0) { ok = 0; break; }
+          if (globaltimer() - t0 > timeout_ns) {
+            raise(ctl, IG_ERR_TIMEOUT);
+            ok = 0;
+            break;
+          }
+        }
+        __nanosleep(32);
+      }
+    }
+    __threadfence();
+    if (ld_relaxed(&ctl->err) != 0) ok = 0;
+    s_ok = ok;
+  }
+  __syncthreads();
+  return s_ok != 0;
+}
+
+// Warp-aggregated append: every lane of a converged warp calls it; lanes with
+// pred append `v` to q.  One atomicAdd per warp.  Returns the number appended.
+__device__ __forceinline__ int warp_append(bool pred, int v, int* q, int* qsize, int cap,
+                                           IgCtl* ctl) {
+  const unsigned m = __ballot_sync(IG_FULL, pred);
+  if (m == 0) return 0;
+  const int lane = lane_id();
+  const int leader = __ffs(m) - 1;
+  int base = 0;
+  if (lane == leader) base = atomicAdd(qsize, __popc(m));
+  base = __shfl_sync(IG_FULL, base, leader);
+  if (pred) {
+    const int pos = base + __popc(m & lanemask_lt());
+    if (pos < cap) q[pos] = v;
+    else raise(ctl, IG_ERR_OVERFLOW);
+  }
+  return __popc(m);
+}
+
+// Same as warp_append, also adding the 64-bit sum of `w` over appending lanes
+// to *wsum (used for the frontier edge count of direction-optimising BFS).
+__device__ __forceinline__ void warp_append_w(bool pred, int v, long long w, int* q, int* qsize,
+                                              unsigned long long* wsum, int cap, IgCtl* ctl) {
+  const unsigned m = __ballot_sync(IG_FULL, pred);
+  if (m == 0) return;
+  long long x = pred ? w : 0;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(IG_FULL, x, o);
+  const int lane = lane_id();
+  const int leader = __ffs(m) - 1;
+  int base = 0;
+  if (lane == leader) {
+    base = atomicAdd(qsize, __popc(m));
+    atomicAdd(wsum, (unsigned long long)x);
+  }
+  base = __shfl_sync(IG_FULL, base, leader);
+  if (pred) {
+    const int pos = base + __popc(m & lanemask_lt());
+    if (pos < cap) q[pos] = v;
+    else raise(ctl, IG_ERR_OVERFLOW);
+  }
+}
+
+// Load-balanced expansion.  Each lane holds one vertex's edge range
+// [beg, beg+deg) (deg may be 0).  The warp walks the concatenation of the 32
+// ranges, 32 edges per step; for edge slot e the owning lane j is found by a
+// 5-step binary search over the exclusive prefix of the degrees.
+// visit(active, edge_index, owner_lane) is called by all 32 lanes every step
+// (warp-uniform), so it may use warp collectives.
+template <class Visit>
+__device__ __forceinline__ void warp_expand(int beg, int deg, Visit&& visit) {
+  const int lane = lane_id();
+  int incl = deg;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int t = __shfl_up_sync(IG_FULL, incl, o);
+    if (lane >= o) incl += t;
+  }
+  const int total = __shfl_sync(IG_FULL, incl, 31);
+  const int excl = incl - deg;
+  for (int base = 0; base < total; base += 32) {
+    const int e = base + lane;
+    int j = 0;
+#pragma unroll
+    for (int step = 16; step >= 1; step >>= 1) {
+      const int ex = __shfl_sync(IG_FULL, excl, j + step);
+      if (ex <= e) j += step;
+    }
+    const int jb = __shfl_sync(IG_FULL, beg, j);
+    const int je = __shfl_sync(IG_FULL, excl, j);
+    visit(e < total, jb + (e - je), j);
+  }
+}
+
+// Block-wide exclusive scan of `n <= blockDim.x * 4` 64-bit values held in
+// shared memory `vals` (in place; vals[n] receives the total).  Requires all
+// threads of the block; `warp_tmp` must hold blockDim.x/32 entries.
+__device__ __forceinline__ void block_exclusive_scan64(long long* vals, int n, long long* warp_tmp) {
+  const int tid = threadIdx.x;
+  const int per = (n + blockDim.x - 1) / blockDim.x;  // <= 4
+  long long local[4];
+  long long sum = 0;
+  for (int k = 0; k < per && k < 4; k++) {
+    const int i = tid * per + k;
+    local[k] = (i < n) ? vals[i] : 0;
+    sum += local[k];
+  }
+  // inclusive scan of per-thread sums
+  const int lane = tid & 31, warp = tid >> 5;
+  long long x = sum;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const long long t = __shfl_up_sync(IG_FULL, x, o);
+    if (lane >= o) x += t;
+  }
+  if (lane == 31) warp_tmp[warp] = x;
+  __syncthreads();
+  if (warp == 0) {
+    const int nw = blockDim.x >> 5;
+    long long w = (lane < nw) ? warp_tmp[lane] : 0;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const long long t = __shfl_up_sync(IG_FULL, w, o);
+      if (lane >= o) w += t;
+    }
+    if (lane < nw) warp_tmp[lane] = w;  // inclusive warp totals
+  }
+  __syncthreads();
+  long long run = x - sum + (warp > 0 ? warp_tmp[warp - 1] : 0);
+  for (int k = 0; k < per && k < 4; k++) {
+    const int i = tid * per + k;
+    if (i < n) vals[i] = run;
+    run += local[k];
+  }
+  if (tid == blockDim.x - 1) vals[n] = run;
+  __syncthreads();
+}
+
+// The reference MIS priority hash (include/mis_vertex_cpp.h:135-140),
+// applied to v + 712313887 with unsigned arithmetic.
+__device__ __forceinline__ unsigned mis_hash(unsigned val) {
+  val = ((val >> 16) ^ val) * 0x45d9f3bu;
+  val = ((val >> 16) ^ val) * 0x45d9f3bu;
+  return (val >> 16) ^ val;
+}
+__device__ __forceinline__ unsigned mis_priority(int v) { return mis_hash((unsigned)v + 712313887u); }
+
+}  // namespace ig
+
+namespace ig {
+
+// Vertices with more neighbours than this are expanded by the whole grid.
+constexpr int kHubBatch = 1024;  // hubs staged per shared-memory pass
+
+// Expands the adjacency lists of the `nh` vertices in `hubs` across every
+// thread of the grid (edge-balanced).  visit(active, edge_index, hub_vertex)
+// is called warp-uniformly.  Requires blockDim.x * 4 >= kHubBatch and all
+// threads of every block.
+template <class Visit>
+__device__ __forceinline__ void grid_expand_hubs(const int* __restrict__ nindex, const int* hubs, int nh,
+                                                 Visit&& visit) {
+  __shared__ long long s_pref[kHubBatch + 1];
+  __shared__ int s_beg[kHubBatch];
+  __shared__ int s_v[kHubBatch];
+  __shared__ long long s_warp[32];
+  const long long gthreads = (long long)gridDim.x * blockDim.x;
+  for (int hb = 0; hb < nh; hb += kHubBatch) {
+    const int cnt = min(kHubBatch, nh - hb);
+    __syncthreads();
+    for (int i = threadIdx.x; i < cnt; i += blockDim.x) {
+      const int v = hubs[hb + i];
+      const int b = __ldg(&nindex[v]);
+      s_v[i] = v;
+      s_beg[i] = b;
+      s_pref[i] = __ldg(&nindex[v + 1]) - b;
+    }
+    __syncthreads();
+    block_exclusive_scan64(s_pref, cnt, s_warp);
+    const long long total = s_pref[cnt];
+    const long long wbase = (long long)blockIdx.x * blockDim.x + (threadIdx.x & ~31);
+    for (long long base = wbase; base < total; base += gthreads) {
+      const long long e = base + lane_id();
+      const bool act = e < total;
+      int h = 0;
+      if (act) {
+        int lo = 0, hi = cnt - 1;  // largest h with s_pref[h] <= e
+        while (lo < hi) {
+          const int mid = (lo + hi + 1) >> 1;
+          if (s_pref[mid] <= e) lo = mid;
+          else hi = mid - 1;
+        }
+        h = lo;
+      }
+      visit(act, act ? s_beg[h] + (int)(e - s_pref[h]) : 0, act ? s_v[h] : 0);
+    }
+  }
+  __syncthreads();
+}
+
+}  // namespace ig
+
+namespace ig {
+
+// Block-wide exclusive scan of one int per thread; returns the thread's
+// exclusive prefix and writes the block total to *total (all threads).
+// `tmp` must hold 33 ints of shared memory.
+__device__ __forceinline__ int block_scan_int(int x, int* tmp, int* total) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  int incl = x;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int t = __shfl_up_sync(IG_FULL, incl, o);
+    if (lane >= o) incl += t;
+  }
+  __syncthreads();
+  if (lane == 31) tmp[warp] = incl;
+  __syncthreads();
+  if (warp == 0) {
+    int w = (lane < nw) ? tmp[lane] : 0;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int t = __shfl_up_sync(IG_FULL, w, o);
+      if (lane >= o) w += t;
+    }
+    if (lane < nw) tmp[lane] = w;
+    if (lane == nw - 1) tmp[32] = w;
+  }
+  __syncthreads();
+  const int res = incl - x + (warp > 0 ? tmp[warp - 1] : 0);
+  *total = tmp[32];
+  return res;
+}
+
+// Block-wide sum of a double with a fixed reduction tree (deterministic);
+// the result is valid in thread 0.  `tmp` must hold 32 doubles.
+__device__ __forceinline__ double block_sum_double(double x, double* tmp) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(IG_FULL, x, o);
+  __syncthreads();
+  if (lane == 0) tmp[warp] = x;
+  __syncthreads();
+  double r = 0;
+  if (warp == 0) {
+    r = (lane < nw) ? tmp[lane] : 0.0;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) r += __shfl_down_sync(IG_FULL, r, o);
+  }
+  return r;
+}
+
+}  // namespace ig

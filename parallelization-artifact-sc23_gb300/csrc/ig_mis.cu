@@ -1,0 +1,173 @@
+// Maximal independent set by priority rounds: one persistent, cooperatively
+// launched kernel per call.
+//
+// Reference rule (codes/cpp/mis-cpp/MIS_CPP_V_Topo_Push_IntType_Atomic_
+// CopyDeterm_Block.cpp:50-73, priorities from include/mis_vertex_cpp.h:135-140
+// applied to v + 712313887 and compared as UNSIGNED int): an undecided vertex
+// joins the set when no non-excluded neighbour has a larger (priority, id);
+// it then excludes all its neighbours; rounds repeat until nothing is
+// undecided.  With fixed priorities that process has exactly one outcome --
+// the greedy set taken in decreasing (priority, id) order: v is in the set iff
+// no larger neighbour is in the set.  Any schedule that (1) includes v only
+// once every larger neighbour is excluded and (2) excludes v only once a
+// neighbour is included reaches that same set, because statuses only ever
+// move from undecided to decided.  This kernel is such a schedule:
+//   - an undecided vertex scans only its LARGER neighbours, starting where its
+//     previous scan stopped (excluded vertices stay excluded): an included one
+//     excludes it, an undecided one blocks it until a later round, and
+//     reaching the end includes it and pushes "excluded" to all neighbours;
+//   - statuses are updated in place (no per-round copy, unlike :89-103);
+//   - the undecided vertices are compacted into a worklist each round
+//     (warp-aggregated append), so later rounds touch only what is left;
+//   - vertices with more than 32 neighbours are scanned 32 at a time by the
+//     whole warp with ballots.
+// The result equals the reference C++ CopyDeterm set bit for bit.  (The CUDA
+// variants compare priorities as signed int and reach a different set.)
+#include "ig_device.cuh"
+#include "ig_options.h"
+
+namespace {
+
+constexpr int kThreads = 256;
+constexpr int kUndecided = 0, kIncluded = 1, kExcluded = 2;
+
+struct MisArgs {
+  const int* __restrict__ nindex;
+  const int* __restrict__ nlist;
+  int nodes;
+  int* status;
+  int* resume;
+  int* wa;
+  int* wb;
+  IgCtl* ctl;
+  unsigned long long timeout_ns;
+};
+
+__device__ __forceinline__ int load_status(const int* s, int v) { return *((const volatile int*)s + v); }
+
+// (pn, n) > (pv, v) in the reference's order
+__device__ __forceinline__ bool larger(unsigned pn, int n, unsigned pv, int v) {
+  return pn > pv || (pn == pv && n > v);
+}
+
+__global__ void __launch_bounds__(kThreads) mis_persistent(MisArgs a) {
+  using namespace ig;
+  IgCtl* ctl = a.ctl;
+  const int lane = lane_id();
+  const long long gtid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long long gthreads = (long long)gridDim.x * blockDim.x;
+
+  for (long long v = gtid; v < a.nodes; v += gthreads) {
+    a.status[v] = kUndecided;
+    a.resume[v] = __ldg(&a.nindex[v]);
+  }
+  if (!grid_sync(ctl, a.timeout_ns)) return;
+
+  int* cur = a.wa;
+  int* nxt = a.wb;
+  int cur_size = a.nodes;  // round 0 walks all vertices directly
+  int round = 0;
+  while (cur_size > 0) {
+    const int slot = round % 3;
+    if (gtid == 0) ctl->i32[(round + 1) % 3] = 0;
+    int* wsize = &ctl->i32[slot];
+    for (long long base = gtid & ~31LL; base < cur_size; base += gthreads) {
+      const long long i = base + lane;
+      int v = 0, beg = 0, end = 0;
+      bool live = false;
+      if (i < cur_size) {
+        v = (round == 0) ? (int)i : cur[i];
+        live = load_status(a.status, v) == kUndecided;
+        beg = a.resume[v];
+        end = __ldg(&a.nindex[v + 1]);
+      }
+      const unsigned pv = mis_priority(v);
+      bool blocked = false;
+      // light vertices: sequential scan by the owning lane
+      const bool light = live && (end - beg) <= 32;
+      if (light) {
+        int outcome = kIncluded;
+        int k = beg;
+        for (; k < end; k++) {
+          const int n = __ldg(&a.nlist[k]);
+          if (larger(mis_priority(n), n, pv, v)) {
+            const int s = load_status(a.status, n);
+            if (s == kIncluded) { outcome = kExcluded; break; }
+            if (s == kUndecided) { outcome = kUndecided; break; }
+          }
+        }
+        if (outcome == kIncluded) {
+          a.status[v] = kIncluded;
+          for (int q = __ldg(&a.nindex[v]); q < end; q++) a.status[__ldg(&a.nlist[q])] = kExcluded;
+        } else if (outcome == kExcluded) {
+          a.status[v] = kExcluded;
+        } else {
+          a.resume[v] = k;
+          blocked = true;
+        }
+      }
+      // heavy vertices: one at a time, the warp scans 32 neighbours per step
+      unsigned heavy = __ballot_sync(IG_FULL, live && !light);
+      while (heavy) {
+        const int src_lane = __ffs(heavy) - 1;
+        heavy &= heavy - 1;
+        const int hv = __shfl_sync(IG_FULL, v, src_lane);
+        const int hb = __shfl_sync(IG_FULL, beg, src_lane);
+        const int he = __shfl_sync(IG_FULL, end, src_lane);
+        const unsigned ph = mis_priority(hv);
+        int outcome = kIncluded, stop = he;
+        for (int k0 = hb; k0 < he; k0 += 32) {
+          const int k = k0 + lane;
+          bool inc = false, und = false;
+          if (k < he) {
+            const int n = __ldg(&a.nlist[k]);
+            if (larger(mis_priority(n), n, ph, hv)) {
+              const int s = load_status(a.status, n);
+              inc = s == kIncluded;
+              und = s == kUndecided;
+            }
+          }
+          const unsigned mi = __ballot_sync(IG_FULL, inc);
+          const unsigned mu = __ballot_sync(IG_FULL, und);
+          if (mi) { outcome = kExcluded; break; }
+          if (mu) { outcome = kUndecided; stop = k0 + __ffs(mu) - 1; break; }
+        }
+        if (outcome == kIncluded) {
+          if (lane == 0) a.status[hv] = kIncluded;
+          const int b0 = __ldg(&a.nindex[hv]);
+          for (int q = b0 + lane; q < he; q += 32) a.status[__ldg(&a.nlist[q])] = kExcluded;
+        } else if (outcome == kExcluded) {
+          if (lane == 0) a.status[hv] = kExcluded;
+        } else {
+          if (lane == 0) a.resume[hv] = stop;
+          if (lane == src_lane) blocked = true;
+        }
+      }
+      warp_append(blocked, v, nxt, wsize, a.nodes, ctl);
+    }
+    if (!grid_sync(ctl, a.timeout_ns)) return;
+    cur_size = ld_relaxed(wsize);
+    round++;
+    int* t = cur;
+    cur = nxt;
+    nxt = t;
+  }
+  if (gtid == 0) ctl->iterations = round;
+}
+
+}  // namespace
+
+int igk_mis(IgExec* ex, const ig_csr* dg, int* d_status, unsigned int* d_prio) {
+  (void)d_prio;
+  const size_t vb = (size_t)dg->nodes * sizeof(int);
+  void *resume, *wa, *wb;
+  int rc;
+  if ((rc = ig_scratch_get(ex->scratch, IG_SLOT_V0, vb, &resume))) return rc;
+  if ((rc = ig_scratch_get(ex->scratch, IG_SLOT_Q0, vb, &wa))) return rc;
+  if ((rc = ig_scratch_get(ex->scratch, IG_SLOT_Q1, vb, &wb))) return rc;
+  if ((rc = ig_exec_reset(ex))) return rc;
+  const IgOptions& o = ig_options();
+  MisArgs a{dg->nindex, dg->nlist, dg->nodes, d_status, (int*)resume, (int*)wa, (int*)wb, ex->d_ctl, ex->timeout_ns};
+  void* args[] = {&a};
+  return ig_launch_coop(ex, (const void*)mis_persistent, kThreads, 0, o.blocks_per_sm, args, nullptr);
+}

@@ -1,0 +1,15 @@
+// Tunable knobs of the kernels (set through ig_set_option; read by launchers).
+#pragma once
+
+struct IgOptions {
+  int blocks_per_sm;      // cap on resident blocks per SM for persistent kernels (0 = occupancy)
+  int bfs_alpha;          // top-down -> bottom-up switch: frontier edges > unexplored / alpha
+  int bfs_beta;           // bottom-up -> top-down switch: frontier vertices < V / beta
+  int hub_degree;         // degree above which a vertex is expanded by the whole grid
+  long long sssp_delta;   // near/far bucket width (0 = derived from sampled weights)
+  int sssp_delta_scale;   // derived width = mean weight * scale / mean degree
+  int pr_hub_degree;      // PageRank: degree above which a vertex is split in chunks
+  int pr_chunk;           // PageRank: edges per hub chunk
+};
+
+IgOptions& ig_options();

@@ -1,0 +1,302 @@
+// PageRank, pull formulation: one persistent, cooperatively launched kernel
+// runs every iteration and tests convergence on the device.
+//
+// Reference semantics (include/pr_cuda.h:42-46, 113-135 and the pull variants,
+// e.g. codes/cuda/pr-cuda/PR_CUDA_Pull_FloatType_Persist_Warp_Determ_
+// Reduction.cu:41-83; C++ codes/cpp/pr-cpp/PR_CPP_Pull_FloatType_Reduction_
+// Block_Determin.cpp:40-89): a Jacobi step
+//     contrib[u] = score[u] / degree[u]
+//     score[v]   = (1 - d) / V + d * sum_{u in N(v)} contrib[u],   d = 0.85
+// with the FP32 L1 change sum |score_new - score_old| accumulated in double;
+// iterations stop when that change is below epsilon or after max_iter.  The
+// reference issues two kernels and two small copies per iteration; here the
+// whole loop runs on the device and the host learns the iteration count.
+//
+// Accuracy: each vertex's incoming sum is accumulated in FP32 with Kahan
+// compensation (lanes of a warp combine their partial sums exactly with
+// TwoSum); the residual is accumulated in FP64 with a fixed reduction tree,
+// so every run of the same input gives bit-identical scores.
+//
+// Work split: 32 consecutive vertices per warp (static schedule).  A vertex
+// with <= kLight neighbours is summed by its own lane, one with more by the
+// whole warp; a vertex above the hub degree is cut into fixed chunks of edges
+// spread over all warps, and its chunk sums are combined in chunk order after
+// a grid barrier.
+#include "ig_device.cuh"
+#include "ig_options.h"
+
+namespace {
+
+constexpr int kThreads = 256;
+constexpr int kLight = 16;
+
+struct PrArgs {
+  const int* __restrict__ nindex;
+  const int* __restrict__ nlist;
+  const int* degree;  // may be null: nindex difference
+  int nodes;
+  long long edges;
+  float* scores;
+  float* ca;          // contributions (alternating)
+  float* cb;
+  int* hubs;          // hub vertices in increasing id order
+  int* chunk_base;    // first chunk of each hub (hubs + 1 entries)
+  float2* partial;    // per-chunk (hi, lo) sums
+  int* blk;           // per-block counts for the deterministic hub compaction (2 * grid)
+  double* blkerr;     // per-block residual partials (2 * grid)
+  IgCtl* ctl;
+  float eps;
+  int max_iter;
+  float base;
+  float damp;
+  unsigned long long timeout_ns;
+  int hub_degree;
+  int chunk;
+};
+
+__device__ __forceinline__ void kahan_add(float& s, float& c, float x) {
+  const float y = __fsub_rn(x, c);
+  const float t = __fadd_rn(s, y);
+  c = __fsub_rn(__fsub_rn(t, s), y);
+  s = t;
+}
+// (hi, lo) += (h2, l2) with an exact TwoSum of the leading parts.
+__device__ __forceinline__ void pair_add(float& hi, float& lo, float h2, float l2) {
+  const float s = __fadd_rn(hi, h2);
+  const float bb = __fsub_rn(s, hi);
+  const float e = __fadd_rn(__fsub_rn(hi, __fsub_rn(s, bb)), __fsub_rn(h2, bb));
+  const float l = __fadd_rn(e, __fadd_rn(lo, l2));
+  const float t = __fadd_rn(s, l);
+  lo = __fsub_rn(l, __fsub_rn(t, s));
+  hi = t;
+}
+__device__ __forceinline__ void warp_pair_reduce(float& hi, float& lo) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const float h2 = __shfl_xor_sync(IG_FULL, hi, o);
+    const float l2 = __shfl_xor_sync(IG_FULL, lo, o);
+    pair_add(hi, lo, h2, l2);
+  }
+}
+
+// Kahan sum of contrib[nlist[k]] over k = b + lane, b + lane + 32, ... < e,
+// returned as a (hi, lo) pair reduced over the warp (same value in all lanes).
+__device__ __forceinline__ void warp_gather_sum(const int* __restrict__ nlist, const float* contrib, int b, int e,
+                                                float& hi, float& lo) {
+  float s = 0.f, c = 0.f;
+  int k = b + ig::lane_id();
+  for (; k + 96 < e; k += 128) {
+    const int n0 = __ldg(&nlist[k]), n1 = __ldg(&nlist[k + 32]);
+    const int n2 = __ldg(&nlist[k + 64]), n3 = __ldg(&nlist[k + 96]);
+    const float x0 = contrib[n0], x1 = contrib[n1], x2 = contrib[n2], x3 = contrib[n3];
+    kahan_add(s, c, x0);
+    kahan_add(s, c, x1);
+    kahan_add(s, c, x2);
+    kahan_add(s, c, x3);
+  }
+  for (; k < e; k += 32) kahan_add(s, c, contrib[__ldg(&nlist[k])]);
+  hi = s;
+  lo = -c;
+  warp_pair_reduce(hi, lo);
+}
+
+__device__ __forceinline__ int vdegree(const PrArgs& a, int v) {
+  return a.degree ? a.degree[v] : (__ldg(&a.nindex[v + 1]) - __ldg(&a.nindex[v]));
+}
+
+__global__ void __launch_bounds__(kThreads) pr_persistent(PrArgs a) {
+  using namespace ig;
+  __shared__ int s_scan[33];
+  __shared__ double s_red[32];
+  IgCtl* ctl = a.ctl;
+  const int lane = lane_id();
+  const int G = gridDim.x;
+  const long long gtid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long long gthreads = (long long)gridDim.x * blockDim.x;
+  const int warp_g = (int)(gtid >> 5);
+  const int nwarps = (int)(gthreads >> 5);
+
+  // ---- initial contributions, hub census per contiguous block range
+  for (long long v = gtid; v < a.nodes; v += gthreads)
+    a.ca[v] = __fdiv_rn(a.scores[v], (float)vdegree(a, (int)v));
+  const long long r0 = (long long)a.nodes * blockIdx.x / G, r1 = (long long)a.nodes * (blockIdx.x + 1) / G;
+  {
+    int nh = 0, nc = 0;
+    for (long long v = r0 + threadIdx.x; v < r1; v += blockDim.x) {
+      const int d = __ldg(&a.nindex[v + 1]) - __ldg(&a.nindex[v]);
+      if (d > a.hub_degree) {
+        nh++;
+        nc += (d + a.chunk - 1) / a.chunk;
+      }
+    }
+    int th, tc;
+    block_scan_int(nh, s_scan, &th);
+    block_scan_int(nc, s_scan, &tc);
+    if (threadIdx.x == 0) {
+      a.blk[blockIdx.x] = th;
+      a.blk[G + blockIdx.x] = tc;
+    }
+  }
+  if (!grid_sync(ctl, a.timeout_ns)) return;
+  // ---- deterministic compaction of the hubs (in vertex order)
+  {
+    int hoff = 0, coff = 0, htot = 0, ctot = 0;
+    for (int b = 0; b < G; b++) {
+      const int h = ld_relaxed(&a.blk[b]), c = ld_relaxed(&a.blk[G + b]);
+      if (b < (int)blockIdx.x) {
+        hoff += h;
+        coff += c;
+      }
+      htot += h;
+      ctot += c;
+    }
+    for (long long t0 = r0; t0 < r1; t0 += blockDim.x) {
+      const long long v = t0 + threadIdx.x;
+      int d = 0;
+      if (v < r1) d = __ldg(&a.nindex[v + 1]) - __ldg(&a.nindex[v]);
+      const bool hub = d > a.hub_degree;
+      const int nc = hub ? (d + a.chunk - 1) / a.chunk : 0;
+      int th, tc;
+      const int ph = block_scan_int(hub ? 1 : 0, s_scan, &th);
+      const int pc = block_scan_int(nc, s_scan, &tc);
+      if (hub) {
+        a.hubs[hoff + ph] = (int)v;
+        a.chunk_base[hoff + ph] = coff + pc;
+      }
+      hoff += th;
+      coff += tc;
+    }
+    if (gtid == 0) {
+      ctl->i32[10] = htot;
+      ctl->i32[11] = ctot;
+      a.chunk_base[htot] = ctot;
+    }
+  }
+  if (!grid_sync(ctl, a.timeout_ns)) return;
+  const int nh = ld_relaxed(&ctl->i32[10]);
+  const int nchunks = ld_relaxed(&ctl->i32[11]);
+
+  float* cur = a.ca;
+  float* nxt = a.cb;
+  int it = 0;
+  double residual = 0;
+  while (it < a.max_iter) {
+    it++;
+    double err = 0;
+    // ---- phase A: hub chunks (partial sums) and regular vertices
+    for (int c = warp_g; c < nchunks; c += nwarps) {
+      // owning hub: largest h with chunk_base[h] <= c
+      int lo = 0, hi = nh - 1;
+      while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (a.chunk_base[mid] <= c) lo = mid;
+        else hi = mid - 1;
+      }
+      const int hv = a.hubs[lo];
+      const int hb = __ldg(&a.nindex[hv]), he = __ldg(&a.nindex[hv + 1]);
+      const int b = hb + (c - a.chunk_base[lo]) * a.chunk;
+      const int e = min(b + a.chunk, he);
+      float shi, slo;
+      warp_gather_sum(a.nlist, cur, b, e, shi, slo);
+      if (lane == 0) a.partial[c] = make_float2(shi, slo);
+    }
+    for (long long base = (long long)warp_g * 32; base < a.nodes; base += (long long)nwarps * 32) {
+      const long long vi = base + lane;
+      int v = (int)vi, b = 0, e = 0;
+      if (vi < a.nodes) {
+        b = __ldg(&a.nindex[v]);
+        e = __ldg(&a.nindex[v + 1]);
+      }
+      const int d = e - b;
+      float sum = 0.f;
+      const bool light = vi < a.nodes && d <= kLight;
+      if (light) {
+        float s = 0.f, c = 0.f;
+        for (int k = b; k < e; k++) kahan_add(s, c, cur[__ldg(&a.nlist[k])]);
+        sum = __fsub_rn(s, c);
+      }
+      unsigned med = __ballot_sync(IG_FULL, vi < a.nodes && d > kLight && d <= a.hub_degree);
+      while (med) {
+        const int l = __ffs(med) - 1;
+        med &= med - 1;
+        const int mb = __shfl_sync(IG_FULL, b, l), me = __shfl_sync(IG_FULL, e, l);
+        float shi, slo;
+        warp_gather_sum(a.nlist, cur, mb, me, shi, slo);
+        if (lane == l) sum = __fadd_rn(shi, slo);
+      }
+      if (vi < a.nodes && d <= a.hub_degree) {
+        const float old = a.scores[v];
+        const float nw = __fadd_rn(a.base, __fmul_rn(a.damp, sum));
+        a.scores[v] = nw;
+        nxt[v] = __fdiv_rn(nw, (float)vdegree(a, v));
+        err += (double)fabsf(__fsub_rn(nw, old));
+      }
+    }
+    // ---- phase B: combine hub chunks in chunk order
+    if (nh > 0) {
+      if (!grid_sync(ctl, a.timeout_ns)) return;
+      for (int h = warp_g; h < nh; h += nwarps) {
+        const int c0 = a.chunk_base[h], c1 = a.chunk_base[h + 1];
+        float hi = 0.f, lo = 0.f;
+        for (int c = c0 + lane; c < c1; c += 32) {
+          const float2 p = a.partial[c];
+          pair_add(hi, lo, p.x, p.y);
+        }
+        warp_pair_reduce(hi, lo);
+        if (lane == 0) {
+          const int v = a.hubs[h];
+          const float sum = __fadd_rn(hi, lo);
+          const float old = a.scores[v];
+          const float nw = __fadd_rn(a.base, __fmul_rn(a.damp, sum));
+          a.scores[v] = nw;
+          nxt[v] = __fdiv_rn(nw, (float)vdegree(a, v));
+          err += (double)fabsf(__fsub_rn(nw, old));
+        }
+      }
+    }
+    const double berr = block_sum_double(err, s_red);
+    double* slot = a.blkerr + (it & 1) * G;
+    if (threadIdx.x == 0) slot[blockIdx.x] = berr;
+    if (!grid_sync(ctl, a.timeout_ns)) return;
+    residual = 0;
+    for (int b = 0; b < G; b++) residual += ld_relaxed(&slot[b]);
+    float* t = cur;
+    cur = nxt;
+    nxt = t;
+    if (residual < (double)a.eps) break;
+  }
+  if (gtid == 0) {
+    ctl->iterations = it;
+    ctl->residual = residual;
+  }
+}
+
+}  // namespace
+
+int igk_pr(IgExec* ex, const ig_csr* dg, const int* d_degree, float* d_scores, float epsilon, int max_iter) {
+  const IgOptions& o = ig_options();
+  const int n = dg->nodes;
+  const int hub_degree = std::max(o.pr_hub_degree, 32);
+  const int chunk = std::max(o.pr_chunk, 32);
+  const long long max_hubs = (long long)dg->edges / (hub_degree + 1) + 1;
+  const long long max_chunks = (long long)dg->edges / chunk + max_hubs + 1;
+  const int max_blocks = ex->sms * 32;
+  void *ca, *cb, *hubs, *cbase, *part, *blk, *blkerr;
+  int rc;
+  if ((rc = ig_scratch_get(ex->scratch, IG_SLOT_F0, (size_t)n * sizeof(float), &ca))) return rc;
+  if ((rc = ig_scratch_get(ex->scratch, IG_SLOT_F1, (size_t)n * sizeof(float), &cb))) return rc;
+  if ((rc = ig_scratch_get(ex->scratch, IG_SLOT_Q0, (size_t)max_hubs * sizeof(int), &hubs))) return rc;
+  if ((rc = ig_scratch_get(ex->scratch, IG_SLOT_Q1, (size_t)(max_hubs + 1) * sizeof(int), &cbase))) return rc;
+  if ((rc = ig_scratch_get(ex->scratch, IG_SLOT_Q2, (size_t)max_chunks * sizeof(float2), &part))) return rc;
+  if ((rc = ig_scratch_get(ex->scratch, IG_SLOT_V0, (size_t)2 * max_blocks * sizeof(int), &blk))) return rc;
+  if ((rc = ig_scratch_get(ex->scratch, IG_SLOT_BLK, (size_t)2 * max_blocks * sizeof(double), &blkerr))) return rc;
+  if ((rc = ig_exec_reset(ex))) return rc;
+  const float damp = 0.85f;
+  const float base = (1.0f - damp) / (float)n;
+  PrArgs a{dg->nindex, dg->nlist, d_degree, n, dg->edges, d_scores, (float*)ca, (float*)cb, (int*)hubs,
+           (int*)cbase, (float2*)part, (int*)blk, (double*)blkerr, ex->d_ctl, epsilon, max_iter, base, damp,
+           ex->timeout_ns, hub_degree, chunk};
+  void* args[] = {&a};
+  int cap = o.blocks_per_sm > 0 ? std::min(o.blocks_per_sm, 32) : 32;
+  return ig_launch_coop(ex, (const void*)pr_persistent, kThreads, 0, cap, args, nullptr);
+}

@@ -1,0 +1,682 @@
+// Runtime around the kernels: per-device state, the grow-only scratch pool,
+// control-block handling, cooperative launches, device-memory plumbing, the
+// drop-in entry points (pointer residency of the reference entry functions)
+// and the device-resident graph API.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <atomic>
+#include <climits>
+#include <cstdio>
+#include <cstring>
+#include <memory>
+#include <mutex>
+#include <vector>
+
+#include "ig_internal.h"
+
+static std::atomic<int> g_timeout_ms{5000};
+static std::atomic<long long> g_launches{0};
+
+void ig_count_launches(int n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
+
+extern "C" int ig_kernel_launches(long long* n) {
+  if (!n) return ig_fail(IG_ERR_INVALID_ARG, "null");
+  *n = g_launches.load();
+  return IG_OK;
+}
+
+unsigned long long ig_timeout_ns() { return (unsigned long long)g_timeout_ms.load() * 1000000ull; }
+
+extern "C" int ig_set_wait_timeout_ms(int ms) {
+  if (ms < 1) return ig_fail(IG_ERR_INVALID_ARG, "timeout must be >= 1 ms");
+  g_timeout_ms.store(ms);
+  return IG_OK;
+}
+
+int ig_cuda_check(int e, const char* what) {
+  if (e == cudaSuccess) return IG_OK;
+  if (e == cudaErrorMemoryAllocation)
+    return ig_fail(IG_ERR_NOMEM, "%s: %s", what, cudaGetErrorString((cudaError_t)e));
+  if (e == cudaErrorNoDevice || e == cudaErrorInsufficientDriver)
+    return ig_fail(IG_ERR_NO_DEVICE, "%s: %s", what, cudaGetErrorString((cudaError_t)e));
+  return ig_fail(IG_ERR_CUDA, "%s: %s", what, cudaGetErrorString((cudaError_t)e));
+}
+#define IG_CU(call)                                  \
+  do {                                               \
+    int _rc = ig_cuda_check((int)(call), #call);     \
+    if (_rc != IG_OK) return _rc;                    \
+  } while (0)
+
+// ---------------------------------------------------------------------------
+// Scratch pool
+// ---------------------------------------------------------------------------
+int ig_scratch_get(IgScratch* s, int slot, size_t bytes, void** out) {
+  if (slot < 0 || slot >= IG_SLOT_COUNT) return ig_fail(IG_ERR_INVALID_ARG, "bad scratch slot");
+  bytes = std::max<size_t>(bytes, 256);
+  if (s->cap[slot] < bytes) {
+    if (s->ptr[slot]) cudaFree(s->ptr[slot]);
+    s->ptr[slot] = nullptr;
+    s->cap[slot] = 0;
+    const size_t want = bytes + bytes / 8;  // headroom for slightly larger graphs
+    void* p = nullptr;
+    IG_CU(cudaMalloc(&p, want));
+    s->ptr[slot] = p;
+    s->cap[slot] = want;
+  }
+  *out = s->ptr[slot];
+  return IG_OK;
+}
+
+void ig_scratch_release(IgScratch* s) {
+  for (int i = 0; i < IG_SLOT_COUNT; i++) {
+    if (s->ptr[i]) cudaFree(s->ptr[i]);
+    s->ptr[i] = nullptr;
+    s->cap[i] = 0;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Per-device state
+// ---------------------------------------------------------------------------
+static std::mutex g_dev_mu;
+static IgDevice* g_devs[64];
+
+int ig_current_device(IgDevice** out) {
+  int dev = 0;
+  IG_CU(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= 64) return ig_fail(IG_ERR_NO_DEVICE, "device id %d out of range", dev);
+  std::lock_guard<std::mutex> lk(g_dev_mu);
+  if (!g_devs[dev]) {
+    std::unique_ptr<IgDevice> d(new IgDevice());
+    d->id = dev;
+    IG_CU(cudaDeviceGetAttribute(&d->sms, cudaDevAttrMultiProcessorCount, dev));
+    IG_CU(cudaStreamCreateWithFlags(&d->stream, cudaStreamNonBlocking));
+    IG_CU(cudaEventCreate(&d->ev0));
+    IG_CU(cudaEventCreate(&d->ev1));
+    IG_CU(cudaMallocHost((void**)&d->h_ctl, sizeof(IgCtl)));
+    d->scratch.device = dev;
+    g_devs[dev] = d.release();
+  }
+  *out = g_devs[dev];
+  return IG_OK;
+}
+
+int ig_exec_init(IgExec* ex, cudaStream_t stream, IgScratch* scratch, IgCtl* h_ctl, int device, int sms) {
+  ex->stream = stream;
+  ex->scratch = scratch;
+  ex->h_ctl = h_ctl;
+  ex->device = device;
+  ex->sms = sms;
+  ex->timeout_ns = ig_timeout_ns();
+  void* p = nullptr;
+  const bool fresh = scratch->ptr[IG_SLOT_CTL] == nullptr;
+  int rc = ig_scratch_get(scratch, IG_SLOT_CTL, sizeof(IgCtl), &p);
+  if (rc) return rc;
+  ex->d_ctl = (IgCtl*)p;
+  if (fresh) IG_CU(cudaMemsetAsync(p, 0, sizeof(IgCtl), stream));
+  return IG_OK;
+}
+
+__global__ void ctl_reset_kernel(IgCtl* ctl) {
+  int* w = (int*)ctl;
+  const int n = (int)(sizeof(IgCtl) / sizeof(int));
+  if (threadIdx.x == 0 && ctl->err != 0 && ctl->sticky_err == 0) ctl->sticky_err = ctl->err;
+  __syncthreads();
+  for (int i = 2 + threadIdx.x; i < n; i += blockDim.x) w[i] = 0;  // everything after sticky_err/pad_
+}
+
+int ig_exec_reset(IgExec* ex) {
+  ctl_reset_kernel<<<1, 128, 0, ex->stream>>>(ex->d_ctl);
+  ig_count_launches(1);
+  return ig_cuda_check((int)cudaGetLastError(), "control block reset");
+}
+
+int ig_exec_finish(IgExec* ex) {
+  IG_CU(cudaMemcpyAsync(ex->h_ctl, ex->d_ctl, sizeof(IgCtl), cudaMemcpyDeviceToHost, ex->stream));
+  IG_CU(cudaStreamSynchronize(ex->stream));
+  const int err = ex->h_ctl->err;
+  if (err == IG_ERR_TIMEOUT) return ig_fail(err, "a device-side wait exceeded %d ms", g_timeout_ms.load());
+  if (err == IG_ERR_OVERFLOW) return ig_fail(err, "a device work queue overflowed");
+  if (err != 0) return ig_fail(err, "device reported status %d", err);
+  return IG_OK;
+}
+
+struct OccKey {
+  const void* k;
+  int dev, threads;
+  size_t smem;
+  int blocks;
+};
+static std::mutex g_occ_mu;
+static std::vector<OccKey> g_occ;
+
+int ig_launch_coop(IgExec* ex, const void* kernel, int threads, size_t smem, int cap, void** args,
+                   int* blocks_out) {
+  int per_sm = -1;
+  {
+    std::lock_guard<std::mutex> lk(g_occ_mu);
+    for (auto& o : g_occ)
+      if (o.k == kernel && o.dev == ex->device && o.threads == threads && o.smem == smem) per_sm = o.blocks;
+  }
+  if (per_sm < 0) {
+    IG_CU(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, smem));
+    std::lock_guard<std::mutex> lk(g_occ_mu);
+    g_occ.push_back({kernel, ex->device, threads, smem, per_sm});
+  }
+  if (per_sm < 1) return ig_fail(IG_ERR_CUDA, "persistent kernel cannot be resident (occupancy 0)");
+  if (cap > 0) per_sm = std::min(per_sm, cap);
+  const int blocks = per_sm * ex->sms;
+  IG_CU(cudaLaunchCooperativeKernel(kernel, dim3(blocks), dim3(threads), args, smem, ex->stream));
+  ig_count_launches(1);
+  if (blocks_out) *blocks_out = blocks;
+  return IG_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Device memory plumbing
+// ---------------------------------------------------------------------------
+extern "C" int ig_device_count(int* n) {
+  if (!n) return ig_fail(IG_ERR_INVALID_ARG, "null");
+  *n = 0;
+  const cudaError_t e = cudaGetDeviceCount(n);
+  if (e != cudaSuccess) {
+    *n = 0;
+    cudaGetLastError();
+    return ig_cuda_check((int)e, "cudaGetDeviceCount");
+  }
+  return IG_OK;
+}
+extern "C" int ig_set_device(int device) {
+  IG_CU(cudaSetDevice(device));
+  return IG_OK;
+}
+extern "C" int ig_device_name(char* buf, int len) {
+  if (!buf || len < 1) return ig_fail(IG_ERR_INVALID_ARG, "null");
+  int dev = 0;
+  IG_CU(cudaGetDevice(&dev));
+  cudaDeviceProp p;
+  IG_CU(cudaGetDeviceProperties(&p, dev));
+  snprintf(buf, (size_t)len, "%s (sm_%d%d, %d SMs)", p.name, p.major, p.minor, p.multiProcessorCount);
+  return IG_OK;
+}
+extern "C" int ig_dev_alloc(void** ptr, size_t bytes) {
+  if (!ptr) return ig_fail(IG_ERR_INVALID_ARG, "null");
+  IG_CU(cudaMalloc(ptr, std::max<size_t>(bytes, 1)));
+  return IG_OK;
+}
+extern "C" int ig_dev_free(void* ptr) {
+  IG_CU(cudaFree(ptr));
+  return IG_OK;
+}
+extern "C" int ig_host_alloc_pinned(void** ptr, size_t bytes) {
+  if (!ptr) return ig_fail(IG_ERR_INVALID_ARG, "null");
+  IG_CU(cudaMallocHost(ptr, std::max<size_t>(bytes, 1)));
+  return IG_OK;
+}
+extern "C" int ig_host_free_pinned(void* ptr) {
+  IG_CU(cudaFreeHost(ptr));
+  return IG_OK;
+}
+static int copy_kind(int kind, cudaMemcpyKind* k) {
+  switch (kind) {
+    case 1: *k = cudaMemcpyHostToDevice; return IG_OK;
+    case 2: *k = cudaMemcpyDeviceToHost; return IG_OK;
+    case 3: *k = cudaMemcpyDeviceToDevice; return IG_OK;
+    default: return ig_fail(IG_ERR_INVALID_ARG, "bad copy kind %d", kind);
+  }
+}
+extern "C" int ig_memcpy(void* dst, const void* src, size_t bytes, int kind) {
+  cudaMemcpyKind k;
+  int rc = copy_kind(kind, &k);
+  if (rc) return rc;
+  if (bytes == 0) return IG_OK;
+  IG_CU(cudaMemcpy(dst, src, bytes, k));
+  return IG_OK;
+}
+extern "C" int ig_memcpy_async(void* dst, const void* src, size_t bytes, int kind, void* stream) {
+  cudaMemcpyKind k;
+  int rc = copy_kind(kind, &k);
+  if (rc) return rc;
+  if (bytes == 0) return IG_OK;
+  IG_CU(cudaMemcpyAsync(dst, src, bytes, k, (cudaStream_t)stream));
+  return IG_OK;
+}
+extern "C" int ig_memset(void* dst, int value, size_t bytes) {
+  IG_CU(cudaMemset(dst, value, bytes));
+  return IG_OK;
+}
+extern "C" int ig_device_synchronize(void) {
+  IG_CU(cudaDeviceSynchronize());
+  return IG_OK;
+}
+extern "C" int ig_csr_upload(const ig_csr* h, ig_csr* d) {
+  if (!h || !d || !h->nindex || h->nodes < 1 || h->edges < 0 || (h->edges > 0 && !h->nlist))
+    return ig_fail(IG_ERR_INVALID_ARG, "ig_csr_upload: bad host graph");
+  ig_csr t{h->nodes, h->edges, nullptr, nullptr, nullptr};
+  const size_t vb = ((size_t)h->nodes + 1) * sizeof(int), eb = std::max<size_t>(1, (size_t)h->edges) * sizeof(int);
+  int rc = ig_cuda_check(cudaMalloc((void**)&t.nindex, vb), "cudaMalloc nindex");
+  if (!rc) rc = ig_cuda_check(cudaMalloc((void**)&t.nlist, eb), "cudaMalloc nlist");
+  if (!rc && h->eweight) rc = ig_cuda_check(cudaMalloc((void**)&t.eweight, eb), "cudaMalloc eweight");
+  if (!rc) rc = ig_cuda_check(cudaMemcpy(t.nindex, h->nindex, vb, cudaMemcpyHostToDevice), "copy nindex");
+  if (!rc && h->edges > 0)
+    rc = ig_cuda_check(cudaMemcpy(t.nlist, h->nlist, (size_t)h->edges * sizeof(int), cudaMemcpyHostToDevice), "copy nlist");
+  if (!rc && h->eweight && h->edges > 0)
+    rc = ig_cuda_check(cudaMemcpy(t.eweight, h->eweight, (size_t)h->edges * sizeof(int), cudaMemcpyHostToDevice),
+                       "copy eweight");
+  if (rc) {
+    cudaFree(t.nindex);
+    cudaFree(t.nlist);
+    cudaFree(t.eweight);
+    return rc;
+  }
+  *d = t;
+  return IG_OK;
+}
+extern "C" int ig_csr_free_device(ig_csr* d) {
+  if (!d) return IG_OK;
+  cudaFree(d->nindex);
+  cudaFree(d->nlist);
+  cudaFree(d->eweight);
+  d->nindex = d->nlist = d->eweight = nullptr;
+  return IG_OK;
+}
+extern "C" int ig_stream_create(void** s) {
+  if (!s) return ig_fail(IG_ERR_INVALID_ARG, "null");
+  IG_CU(cudaStreamCreateWithFlags((cudaStream_t*)s, cudaStreamNonBlocking));
+  return IG_OK;
+}
+extern "C" int ig_stream_destroy(void* s) {
+  IG_CU(cudaStreamDestroy((cudaStream_t)s));
+  return IG_OK;
+}
+extern "C" int ig_stream_synchronize(void* s) {
+  IG_CU(cudaStreamSynchronize((cudaStream_t)s));
+  return IG_OK;
+}
+extern "C" int ig_event_create(void** ev) {
+  if (!ev) return ig_fail(IG_ERR_INVALID_ARG, "null");
+  IG_CU(cudaEventCreate((cudaEvent_t*)ev));
+  return IG_OK;
+}
+extern "C" int ig_event_destroy(void* ev) {
+  IG_CU(cudaEventDestroy((cudaEvent_t)ev));
+  return IG_OK;
+}
+extern "C" int ig_event_record(void* ev, void* stream) {
+  IG_CU(cudaEventRecord((cudaEvent_t)ev, (cudaStream_t)stream));
+  return IG_OK;
+}
+extern "C" int ig_event_elapsed_ms(void* a, void* b, float* ms) {
+  if (!ms) return ig_fail(IG_ERR_INVALID_ARG, "null");
+  IG_CU(cudaEventSynchronize((cudaEvent_t)b));
+  IG_CU(cudaEventElapsedTime(ms, (cudaEvent_t)a, (cudaEvent_t)b));
+  return IG_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Drop-in entry points
+// ---------------------------------------------------------------------------
+static int check_dev_graph(const ig_csr* g, bool need_w) {
+  if (!g) return ig_fail(IG_ERR_INVALID_ARG, "null graph");
+  if (g->nodes < 1 || g->edges < 0) return ig_fail(IG_ERR_INVALID_ARG, "node or edge count too low");
+  if (!g->nindex || (g->edges > 0 && !g->nlist)) return ig_fail(IG_ERR_INVALID_ARG, "null graph arrays");
+  if (need_w && g->edges > 0 && !g->eweight) return ig_fail(IG_ERR_INVALID_ARG, "graph has no edge weights");
+  return IG_OK;
+}
+
+// Runs `body(ex, d_out)` on the device's stream between two events and copies
+// `out_bytes` of the result back to `h_out`.
+// `pre(ex, d_out)` runs before the timed region (uploads the reference entry
+// functions do before their timers start).
+struct NoPre {
+  int operator()(IgExec*, void*) const { return IG_OK; }
+};
+template <class Body, class Pre = NoPre>
+static int run_dropin(size_t out_bytes, void* h_out, double* seconds, Body&& body, Pre pre = Pre(),
+                      IgCtl* ctl_copy = nullptr) {
+  IgDevice* dev = nullptr;
+  int rc = ig_current_device(&dev);
+  if (rc) return rc;
+  std::lock_guard<std::mutex> lk(dev->mu);
+  IgExec ex;
+  rc = ig_exec_init(&ex, dev->stream, &dev->scratch, dev->h_ctl, dev->id, dev->sms);
+  if (rc) return rc;
+  void* d_out = nullptr;
+  if (out_bytes) {
+    rc = ig_scratch_get(&dev->scratch, IG_SLOT_OUT, out_bytes, &d_out);
+    if (rc) return rc;
+  }
+  rc = pre(&ex, d_out);
+  if (rc) return rc;
+  IG_CU(cudaEventRecord(dev->ev0, dev->stream));
+  rc = body(&ex, d_out);
+  if (rc) {
+    cudaStreamSynchronize(dev->stream);
+    return rc;
+  }
+  IG_CU(cudaEventRecord(dev->ev1, dev->stream));
+  rc = ig_exec_finish(&ex);
+  if (ctl_copy) memcpy(ctl_copy, dev->h_ctl, sizeof(IgCtl));
+  if (rc) return rc;
+  float ms = 0;
+  IG_CU(cudaEventElapsedTime(&ms, dev->ev0, dev->ev1));
+  if (seconds) *seconds = ms * 1e-3;
+  if (out_bytes && h_out) IG_CU(cudaMemcpy(h_out, d_out, out_bytes, cudaMemcpyDeviceToHost));
+  return IG_OK;
+}
+
+extern "C" int ig_bfs_vertex(int src, const ig_csr* d_g, int* h_dist, double* seconds) {
+  int rc = check_dev_graph(d_g, false);
+  if (rc) return rc;
+  if (!h_dist) return ig_fail(IG_ERR_INVALID_ARG, "null dist");
+  if (src < 0 || src >= d_g->nodes) return ig_fail(IG_ERR_INVALID_ARG, "source %d out of range", src);
+  return run_dropin((size_t)d_g->nodes * sizeof(int), h_dist, seconds,
+                    [&](IgExec* ex, void* out) { return igk_bfs(ex, d_g, src, (int*)out); });
+}
+
+extern "C" int ig_sssp_vertex(int src, const ig_csr* d_g, int* h_dist, double* seconds) {
+  int rc = check_dev_graph(d_g, true);
+  if (rc) return rc;
+  if (!h_dist) return ig_fail(IG_ERR_INVALID_ARG, "null dist");
+  if (src < 0 || src >= d_g->nodes) return ig_fail(IG_ERR_INVALID_ARG, "source %d out of range", src);
+  return run_dropin((size_t)d_g->nodes * sizeof(int), h_dist, seconds,
+                    [&](IgExec* ex, void* out) { return igk_sssp(ex, d_g, src, (int*)out); });
+}
+
+extern "C" int ig_cc_vertex(const ig_csr* d_g, int* h_label, double* seconds) {
+  int rc = check_dev_graph(d_g, false);
+  if (rc) return rc;
+  if (!h_label) return ig_fail(IG_ERR_INVALID_ARG, "null label");
+  return run_dropin((size_t)d_g->nodes * sizeof(int), h_label, seconds,
+                    [&](IgExec* ex, void* out) { return igk_cc(ex, d_g, (int*)out); });
+}
+
+extern "C" int ig_mis_vertex(const ig_csr* d_g, unsigned int* h_priority, int* h_status, double* seconds) {
+  int rc = check_dev_graph(d_g, false);
+  if (rc) return rc;
+  if (!h_status) return ig_fail(IG_ERR_INVALID_ARG, "null status");
+  rc = run_dropin((size_t)d_g->nodes * sizeof(int), h_status, seconds,
+                  [&](IgExec* ex, void* out) { return igk_mis(ex, d_g, (int*)out, nullptr); });
+  if (rc) return rc;
+  if (h_priority) {
+    // The priorities are a pure function of the vertex id.
+    for (int v = 0; v < d_g->nodes; v++) {
+      unsigned x = (unsigned)v + 712313887u;
+      x = ((x >> 16) ^ x) * 0x45d9f3bu;
+      x = ((x >> 16) ^ x) * 0x45d9f3bu;
+      h_priority[v] = (x >> 16) ^ x;
+    }
+  }
+  return IG_OK;
+}
+
+extern "C" int ig_pr(const ig_csr* h_g, float* h_scores, const int* h_degree, float epsilon, int max_iter,
+                     int* iterations, double* seconds) {
+  if (!h_g || !h_scores || !h_g->nindex || h_g->nodes < 1 || h_g->edges < 0 || (h_g->edges > 0 && !h_g->nlist))
+    return ig_fail(IG_ERR_INVALID_ARG, "ig_pr: bad host graph");
+  if (max_iter < 1) return ig_fail(IG_ERR_INVALID_ARG, "max_iter must be >= 1");
+  const size_t vb = ((size_t)h_g->nodes + 1) * sizeof(int), eb = (size_t)h_g->edges * sizeof(int);
+  const size_t sb = (size_t)h_g->nodes * sizeof(float);
+  ig_csr d{h_g->nodes, h_g->edges, nullptr, nullptr, nullptr};
+  int* d_degree = nullptr;
+  IgCtl snapshot;
+  // PR_GPU uploads the graph, degrees and scores itself before its timer
+  // starts (e.g. codes/cuda/pr-cuda/PR_CUDA_Pull_FloatType_Persist_Warp_Determ_Reduction.cu:94-105).
+  auto pre = [&](IgExec* ex, void* out) {
+    void *a, *b, *c;
+    int r;
+    if ((r = ig_scratch_get(ex->scratch, IG_SLOT_G0, vb, &a))) return r;
+    if ((r = ig_scratch_get(ex->scratch, IG_SLOT_G1, eb, &b))) return r;
+    if ((r = ig_scratch_get(ex->scratch, IG_SLOT_G2, vb, &c))) return r;
+    d.nindex = (int*)a;
+    d.nlist = (int*)b;
+    d_degree = h_degree ? (int*)c : nullptr;
+    if ((r = ig_cuda_check(cudaMemcpyAsync(d.nindex, h_g->nindex, vb, cudaMemcpyHostToDevice, ex->stream), "copy nindex")))
+      return r;
+    if (eb && (r = ig_cuda_check(cudaMemcpyAsync(d.nlist, h_g->nlist, eb, cudaMemcpyHostToDevice, ex->stream), "copy nlist")))
+      return r;
+    if (d_degree && (r = ig_cuda_check(cudaMemcpyAsync(d_degree, h_degree, (size_t)h_g->nodes * sizeof(int),
+                                                         cudaMemcpyHostToDevice, ex->stream), "copy degree")))
+      return r;
+    return ig_cuda_check(cudaMemcpyAsync(out, h_scores, sb, cudaMemcpyHostToDevice, ex->stream), "copy scores");
+  };
+  int rc = run_dropin(
+      sb, h_scores, seconds,
+      [&](IgExec* ex, void* out) { return igk_pr(ex, &d, d_degree, (float*)out, epsilon, max_iter); }, pre,
+      &snapshot);
+  if (rc) return rc;
+  if (iterations) *iterations = snapshot.iterations;
+  return IG_OK;
+}
+
+extern "C" int ig_tc_vertex(long long* count, int nodes, const int* d_nindex, const int* d_nlist, double* seconds) {
+  if (!count || nodes < 1 || !d_nindex) return ig_fail(IG_ERR_INVALID_ARG, "ig_tc_vertex: bad argument");
+  int edges = 0;
+  IG_CU(cudaMemcpy(&edges, d_nindex + nodes, sizeof(int), cudaMemcpyDeviceToHost));
+  if (edges < 0 || (edges > 0 && !d_nlist)) return ig_fail(IG_ERR_INVALID_ARG, "bad edge count");
+  unsigned long long c = 0;
+  int rc = run_dropin(sizeof(unsigned long long), &c, seconds, [&](IgExec* ex, void* out) {
+    return igk_tc(ex, nodes, edges, d_nindex, d_nlist, (unsigned long long*)out);
+  });
+  if (rc) return rc;
+  *count = (long long)c;
+  return IG_OK;
+}
+
+// Edge-centric forms: the sp (COO source) array carries no information the
+// CSR does not, so they share the vertex kernels and give identical results.
+extern "C" int ig_bfs_edge(int src, const ig_csr* d_g, int* h_dist, const int* h_sp, double* seconds) {
+  if (d_g && d_g->edges > 0 && !h_sp) return ig_fail(IG_ERR_INVALID_ARG, "null sp");
+  return ig_bfs_vertex(src, d_g, h_dist, seconds);
+}
+extern "C" int ig_sssp_edge(int src, const ig_csr* d_g, int* h_dist, const int* h_sp, double* seconds) {
+  if (d_g && d_g->edges > 0 && !h_sp) return ig_fail(IG_ERR_INVALID_ARG, "null sp");
+  return ig_sssp_vertex(src, d_g, h_dist, seconds);
+}
+extern "C" int ig_cc_edge(const ig_csr* d_g, int* h_label, const int* h_sp, double* seconds) {
+  if (d_g && d_g->edges > 0 && !h_sp) return ig_fail(IG_ERR_INVALID_ARG, "null sp");
+  return ig_cc_vertex(d_g, h_label, seconds);
+}
+extern "C" int ig_mis_edge(const ig_csr* d_g, const int* d_sp, unsigned int* h_priority, int* h_status,
+                           double* seconds) {
+  if (d_g && d_g->edges > 0 && !d_sp) return ig_fail(IG_ERR_INVALID_ARG, "null sp");
+  return ig_mis_vertex(d_g, h_priority, h_status, seconds);
+}
+extern "C" int ig_tc_edge(long long* count, int edges, const int* d_nindex, const int* d_nlist, const int* d_sp,
+                          double* seconds) {
+  (void)edges;
+  if (!d_sp && edges > 0) return ig_fail(IG_ERR_INVALID_ARG, "null sp");
+  // The node count is not an argument of the edge form (include/tc_edge_cuda.h:42);
+  // it is recovered from sp, whose last entry is the largest source vertex.
+  if (edges <= 0) {
+    *count = 0;
+    if (seconds) *seconds = 0;
+    return IG_OK;
+  }
+  int last = 0;
+  IG_CU(cudaMemcpy(&last, d_sp + edges - 1, sizeof(int), cudaMemcpyDeviceToHost));
+  int nodes = last + 1;
+  // vertices after the last one with edges have empty lists: nindex[nodes] == edges
+  return ig_tc_vertex(count, nodes, d_nindex, d_nlist, seconds);
+}
+
+// ---------------------------------------------------------------------------
+// Device-resident graph API
+// ---------------------------------------------------------------------------
+struct ig_graph {
+  ig_csr g;
+  int device = 0;
+  int sms = 0;
+  cudaStream_t stream = nullptr;
+  IgScratch scratch;
+  IgCtl* h_ctl = nullptr;
+  int last_rc = IG_OK;
+  bool pending = false;
+  IgExec ex;
+};
+
+extern "C" int ig_graph_create(const ig_csr* d_g, ig_graph** out) {
+  int rc = check_dev_graph(d_g, false);
+  if (rc) return rc;
+  if (!out) return ig_fail(IG_ERR_INVALID_ARG, "null out");
+  std::unique_ptr<ig_graph> h(new ig_graph());
+  h->g = *d_g;
+  IG_CU(cudaGetDevice(&h->device));
+  IG_CU(cudaDeviceGetAttribute(&h->sms, cudaDevAttrMultiProcessorCount, h->device));
+  IG_CU(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
+  IG_CU(cudaMallocHost((void**)&h->h_ctl, sizeof(IgCtl)));
+  memset(h->h_ctl, 0, sizeof(IgCtl));
+  h->scratch.device = h->device;
+  rc = ig_exec_init(&h->ex, h->stream, &h->scratch, h->h_ctl, h->device, h->sms);
+  if (rc) return rc;
+  *out = h.release();
+  return IG_OK;
+}
+
+extern "C" int ig_graph_destroy(ig_graph* g) {
+  if (!g) return IG_OK;
+  cudaStreamSynchronize(g->stream);
+  ig_scratch_release(&g->scratch);
+  cudaFreeHost(g->h_ctl);
+  cudaStreamDestroy(g->stream);
+  delete g;
+  return IG_OK;
+}
+
+extern "C" int ig_graph_stream(ig_graph* g, void** stream) {
+  if (!g || !stream) return ig_fail(IG_ERR_INVALID_ARG, "null");
+  *stream = (void*)g->ex.stream;
+  return IG_OK;
+}
+
+extern "C" int ig_graph_set_stream(ig_graph* g, void* stream) {
+  if (!g) return ig_fail(IG_ERR_INVALID_ARG, "null graph handle");
+  if (g->pending) {
+    const int rc = ig_exec_finish(&g->ex);
+    g->pending = false;
+    g->last_rc = rc;
+  }
+  g->ex.stream = stream ? (cudaStream_t)stream : g->stream;
+  return IG_OK;
+}
+
+extern "C" int ig_graph_last_run(ig_graph* g, ig_run_info* info) {
+  if (!g || !info) return ig_fail(IG_ERR_INVALID_ARG, "null");
+  int rc = g->last_rc;
+  if (g->pending) {
+    rc = ig_exec_finish(&g->ex);
+    g->pending = false;
+    g->last_rc = rc;
+  }
+  // an error of an earlier asynchronous call on this graph wins
+  if (rc == IG_OK && g->h_ctl->sticky_err != 0) rc = g->h_ctl->sticky_err;
+  if (g->h_ctl->sticky_err != 0) {
+    const int zero = 0;
+    IG_CU(cudaMemcpyAsync(&g->ex.d_ctl->sticky_err, &zero, sizeof(int), cudaMemcpyHostToDevice, g->ex.stream));
+    IG_CU(cudaStreamSynchronize(g->ex.stream));
+  }
+  info->status = rc;
+  info->iterations = g->h_ctl->iterations;
+  info->work = g->h_ctl->work;
+  info->residual = g->h_ctl->residual;
+  return IG_OK;
+}
+
+template <class Body>
+static int graph_run(ig_graph* g, Body&& body) {
+  if (!g) return ig_fail(IG_ERR_INVALID_ARG, "null graph handle");
+  g->ex.timeout_ns = ig_timeout_ns();
+  const int rc = body(&g->ex);
+  g->last_rc = rc;
+  g->pending = (rc == IG_OK);
+  return rc;
+}
+
+extern "C" int ig_bfs(ig_graph* g, int src, int* d_dist) {
+  if (g && (src < 0 || src >= g->g.nodes)) return ig_fail(IG_ERR_INVALID_ARG, "source out of range");
+  if (!d_dist) return ig_fail(IG_ERR_INVALID_ARG, "null dist");
+  return graph_run(g, [&](IgExec* ex) { return igk_bfs(ex, &g->g, src, d_dist); });
+}
+extern "C" int ig_sssp(ig_graph* g, int src, int* d_dist) {
+  if (g && (src < 0 || src >= g->g.nodes)) return ig_fail(IG_ERR_INVALID_ARG, "source out of range");
+  if (g && g->g.edges > 0 && !g->g.eweight) return ig_fail(IG_ERR_INVALID_ARG, "graph has no edge weights");
+  if (!d_dist) return ig_fail(IG_ERR_INVALID_ARG, "null dist");
+  return graph_run(g, [&](IgExec* ex) { return igk_sssp(ex, &g->g, src, d_dist); });
+}
+extern "C" int ig_cc(ig_graph* g, int* d_label) {
+  if (!d_label) return ig_fail(IG_ERR_INVALID_ARG, "null label");
+  return graph_run(g, [&](IgExec* ex) { return igk_cc(ex, &g->g, d_label); });
+}
+extern "C" int ig_mis(ig_graph* g, int* d_status) {
+  if (!d_status) return ig_fail(IG_ERR_INVALID_ARG, "null status");
+  return graph_run(g, [&](IgExec* ex) { return igk_mis(ex, &g->g, d_status, nullptr); });
+}
+extern "C" int ig_pagerank(ig_graph* g, float* d_scores, float epsilon, int max_iter) {
+  if (!d_scores || max_iter < 1) return ig_fail(IG_ERR_INVALID_ARG, "bad PageRank argument");
+  return graph_run(g, [&](IgExec* ex) { return igk_pr(ex, &g->g, nullptr, d_scores, epsilon, max_iter); });
+}
+extern "C" int ig_tc(ig_graph* g, unsigned long long* d_count) {
+  if (!d_count) return ig_fail(IG_ERR_INVALID_ARG, "null count");
+  return graph_run(g, [&](IgExec* ex) {
+    return igk_tc(ex, g->g.nodes, g->g.edges, g->g.nindex, g->g.nlist, d_count);
+  });
+}
+
+// ---------------------------------------------------------------------------
+// Tunable options
+// ---------------------------------------------------------------------------
+#include "ig_options.h"
+
+IgOptions& ig_options() {
+  static IgOptions o{
+      /*blocks_per_sm=*/4,
+      /*bfs_alpha=*/14,
+      /*bfs_beta=*/24,
+      /*hub_degree=*/2048,
+      /*sssp_delta=*/0,
+      /*sssp_delta_scale=*/32,
+      /*pr_hub_degree=*/4096,
+      /*pr_chunk=*/4096,
+  };
+  return o;
+}
+
+struct OptField {
+  const char* name;
+  long long lo, hi;
+  void (*set)(IgOptions&, long long);
+  long long (*get)(const IgOptions&);
+};
+#define IG_OPT(field, lo, hi)                                                      \
+  {#field, lo, hi, [](IgOptions& o, long long v) { o.field = (decltype(o.field))v; }, \
+   [](const IgOptions& o) { return (long long)o.field; }}
+static const OptField g_opt_fields[] = {
+    IG_OPT(blocks_per_sm, 0, 32),     IG_OPT(bfs_alpha, 1, 1000000),   IG_OPT(bfs_beta, 1, 1000000),
+    IG_OPT(hub_degree, 32, INT_MAX),  IG_OPT(sssp_delta, 0, INT_MAX),  IG_OPT(sssp_delta_scale, 1, 1 << 20),
+    IG_OPT(pr_hub_degree, 32, INT_MAX), IG_OPT(pr_chunk, 32, 1 << 24),
+};
+
+extern "C" int ig_set_option(const char* name, long long value) {
+  if (!name) return ig_fail(IG_ERR_INVALID_ARG, "null option name");
+  for (const auto& f : g_opt_fields) {
+    if (strcmp(f.name, name) == 0) {
+      if (value < f.lo || value > f.hi)
+        return ig_fail(IG_ERR_INVALID_ARG, "option %s out of range [%lld, %lld]", name, f.lo, f.hi);
+      f.set(ig_options(), value);
+      return IG_OK;
+    }
+  }
+  return ig_fail(IG_ERR_INVALID_ARG, "unknown option %s", name);
+}
+
+extern "C" int ig_get_option(const char* name, long long* value) {
+  if (!name || !value) return ig_fail(IG_ERR_INVALID_ARG, "null argument");
+  for (const auto& f : g_opt_fields) {
+    if (strcmp(f.name, name) == 0) {
+      *value = f.get(ig_options());
+      return IG_OK;
+    }
+  }
+  return ig_fail(IG_ERR_INVALID_ARG, "unknown option %s", name);
+}

@@ -1,0 +1,243 @@
+// Single-source shortest paths with int32 weights: one persistent,
+// cooperatively launched kernel per call running a near/far worklist
+// (two-bucket delta stepping).  Replaces the per-round host loop of the
+// reference's worklist variants (e.g. codes/cuda/sssp-cuda/SSSP_CUDA_V_Data_
+// Push_Determ_IntType_ReadModifyWrite_NonPersist_CudaAtomic_Thread_
+// NoBoundsBug2_NoBoundsBug1_NonDup.cu:62-126), whose relaxation is
+// `atomicMin(&dist[dst], dist[src] + eweight[i])` and whose worklist is
+// de-duplicated with a per-vertex iteration stamp (atomicMax(&time[dst], iter)).
+//
+// Output semantics follow include/sssp_vertex_cuda.h: shortest distance,
+// INT_MAX if unreachable (checked there against CPUserialDijkstra, :74-99).
+//
+// Near phase: the near queue is expanded 32 vertices per warp (hubs by the
+// whole grid); an improved vertex with distance < T joins the next near queue
+// (once per iteration, by stamp) and otherwise the far pile (once per epoch,
+// by flag).  When the near queue runs dry the far pile is split: the minimum
+// pending distance m is found, T becomes max(T, m) + delta, entries below the
+// old T are stale (already settled through the near queue) and dropped,
+// entries below the new T form the next near queue, the rest stay far.
+#include "ig_device.cuh"
+#include "ig_options.h"
+
+namespace {
+
+constexpr int kThreads = 256;
+constexpr int kDeltaSamples = 4096;
+
+struct SsspArgs {
+  const int* __restrict__ nindex;
+  const int* __restrict__ nlist;
+  const int* __restrict__ eweight;
+  int nodes;
+  long long edges;
+  int src;
+  int* dist;
+  int* qa;       // near queues
+  int* qb;
+  int* fa;       // far piles (alternating by epoch)
+  int* fb;
+  int* stamp;    // near-queue membership stamp
+  int* farflag;  // far-pile membership (epoch + 1)
+  int* hubs;
+  IgCtl* ctl;
+  unsigned long long timeout_ns;
+  int hub_degree;
+  long long delta;       // > 0: fixed bucket width
+  int delta_scale;
+};
+
+// ctl->i32[k % 3]  size of the near queue processed by near iteration k
+// ctl->i32[3 + s]  hub count of near iteration with s = k % 3
+// ctl->i32[6 + f]  far-pile size of epoch with slot f = epoch % 3
+// ctl->u64[4 + f]  minimum pending distance of that epoch's pile
+// ctl->u64[0..1]   weight-sample sum / count, ctl->u64[2] bucket width
+// ctl->work        relaxations that improved a distance
+
+__global__ void __launch_bounds__(kThreads) sssp_persistent(SsspArgs a) {
+  using namespace ig;
+  IgCtl* ctl = a.ctl;
+  const int lane = lane_id();
+  const long long gtid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long long gthreads = (long long)gridDim.x * blockDim.x;
+  const int warp_g = (int)(gtid >> 5);
+  const int nwarps = (int)(gthreads >> 5);
+
+  for (long long v = gtid; v < a.nodes; v += gthreads) {
+    a.dist[v] = (v == a.src) ? 0 : kInf;
+    a.stamp[v] = 0;
+    a.farflag[v] = 0;
+  }
+  if (gtid < kDeltaSamples && a.edges > 0) {
+    const long long e = gtid * a.edges / kDeltaSamples;
+    atomicAdd(&ctl->u64[0], (unsigned long long)max(0, __ldg(&a.eweight[e])));
+    atomicAdd(&ctl->u64[1], 1ull);
+  }
+  if (gtid == 0) {
+    a.qa[0] = a.src;
+    ctl->u64[4] = ctl->u64[5] = ctl->u64[6] = ~0ull;
+  }
+  if (!grid_sync(ctl, a.timeout_ns)) return;
+
+  long long delta = a.delta;
+  if (delta <= 0) {
+    const unsigned long long cnt = ld_relaxed(&ctl->u64[1]);
+    const double mean_w = cnt ? (double)ld_relaxed(&ctl->u64[0]) / (double)cnt : 1.0;
+    const double mean_deg = a.nodes ? (double)a.edges / (double)a.nodes : 1.0;
+    delta = (long long)(mean_w * a.delta_scale / (mean_deg > 1.0 ? mean_deg : 1.0));
+    if (delta < 1) delta = 1;
+  }
+  if (gtid == 0) ctl->u64[2] = (unsigned long long)delta;
+
+  int* cur = a.qa;
+  int* nxt = a.qb;
+  int cur_size = 1;
+  long long T = delta;  // distances < T are near
+  int it = 0;           // near iteration index (stamp it+1 marks the next queue)
+  int epoch = 0;
+  long long improved = 0;
+
+  while (true) {
+    // ------------------------------------------------------------ near phase
+    while (cur_size > 0) {
+      // queue for iteration k: counter slot k % 3; iteration k appends to
+      // slot (k+1) % 3 and clears slot (k+2) % 3 (last read two iterations ago)
+      if (gtid == 0) {
+        ctl->i32[(it + 2) % 3] = 0;
+        ctl->i32[3 + (it + 1) % 3] = 0;
+      }
+      int* qsize = &ctl->i32[(it + 1) % 3];
+      int* nhub = &ctl->i32[3 + it % 3];
+      int* far = (epoch & 1) ? a.fb : a.fa;
+      int* fsize = &ctl->i32[6 + epoch % 3];
+      const int next_stamp = it + 1;
+      const int far_mark = epoch + 1;
+      auto relax = [&](bool act, int e, int du) {
+        bool to_near = false, to_far = false;
+        int v = 0;
+        if (act && du != kInf) {
+          v = __ldg(&a.nlist[e]);
+          const long long nd = (long long)du + __ldg(&a.eweight[e]);
+          if (nd < (long long)a.dist[v]) {
+            const int ndi = (int)nd;
+            const int old = atomicMin(&a.dist[v], ndi);
+            if (ndi < old) {
+              improved++;
+              if (nd < T) to_near = atomicExch(&a.stamp[v], next_stamp) != next_stamp;
+              else to_far = atomicExch(&a.farflag[v], far_mark) != far_mark;
+            }
+          }
+        }
+        warp_append(to_near, v, nxt, qsize, a.nodes, ctl);
+        warp_append(to_far, v, far, fsize, a.nodes, ctl);
+      };
+      for (int base = warp_g * 32; base < cur_size; base += nwarps * 32) {
+        const int i = base + lane;
+        int u = 0, beg = 0, deg = 0, du = kInf;
+        if (i < cur_size) {
+          u = cur[i];
+          beg = __ldg(&a.nindex[u]);
+          deg = __ldg(&a.nindex[u + 1]) - beg;
+          du = a.dist[u];
+        }
+        const bool hub = deg > a.hub_degree;
+        warp_append(hub, u, a.hubs, nhub, a.nodes, ctl);
+        warp_expand(beg, hub ? 0 : deg, [&](bool act, int e, int j) {
+          const int duj = __shfl_sync(IG_FULL, du, j);
+          relax(act, e, duj);
+        });
+      }
+      if (!grid_sync(ctl, a.timeout_ns)) return;
+      const int nh = ld_relaxed(nhub);
+      if (nh > 0) {
+        grid_expand_hubs(a.nindex, a.hubs, nh, [&](bool act, int e, int hv) {
+          relax(act, e, act ? a.dist[hv] : kInf);
+        });
+        if (!grid_sync(ctl, a.timeout_ns)) return;
+      }
+      cur_size = ld_relaxed(qsize);
+      it++;
+      int* t = cur;
+      cur = nxt;
+      nxt = t;
+    }
+    // ------------------------------------------------------------ far split
+    // The near queue for iteration `it` is built in `cur` with counter slot
+    // it % 3 (iteration it-1 appended nothing to it) and stamp `it`.
+    bool done = false;
+    while (cur_size == 0) {
+      const int f = epoch % 3;
+      const int fsz = ld_relaxed(&ctl->i32[6 + f]);
+      if (fsz == 0) {
+        done = true;
+        break;
+      }
+      int* far = (epoch & 1) ? a.fb : a.fa;
+      int* far_next = (epoch & 1) ? a.fa : a.fb;
+      if (gtid == 0) {
+        ctl->i32[6 + (epoch + 1) % 3] = 0;
+        ctl->u64[4 + (epoch + 1) % 3] = ~0ull;
+      }
+      for (long long i = gtid; i < fsz; i += gthreads) {
+        const int d = a.dist[far[i]];
+        if ((long long)d >= T) atomicMin(&ctl->u64[4 + f], (unsigned long long)d);
+      }
+      if (!grid_sync(ctl, a.timeout_ns)) return;
+      const unsigned long long mfar = ld_relaxed(&ctl->u64[4 + f]);
+      const long long T_old = T;
+      if (mfar != ~0ull) T = ((long long)mfar > T ? (long long)mfar : T) + delta;
+      else T = T + delta;
+      int* qsize = &ctl->i32[it % 3];
+      int* fsize_next = &ctl->i32[6 + (epoch + 1) % 3];
+      for (long long base = gtid & ~31LL; base < fsz; base += gthreads) {
+        const long long i = base + lane;
+        bool to_near = false, to_far = false;
+        int v = 0;
+        if (i < fsz) {
+          v = far[i];
+          const long long d = a.dist[v];
+          if (d >= T_old) {
+            if (d < T) to_near = atomicExch(&a.stamp[v], it) != it;
+            else {
+              to_far = true;
+              a.farflag[v] = epoch + 2;
+            }
+          }
+        }
+        warp_append(to_near, v, cur, qsize, a.nodes, ctl);
+        warp_append(to_far, v, far_next, fsize_next, a.nodes, ctl);
+      }
+      if (!grid_sync(ctl, a.timeout_ns)) return;
+      epoch++;
+      cur_size = ld_relaxed(qsize);
+    }
+    if (done) break;
+  }
+  if (improved) atomicAdd((unsigned long long*)&ctl->work, (unsigned long long)improved);
+  if (gtid == 0) {
+    ctl->iterations = it;
+    ctl->i32[20] = epoch;
+  }
+}
+
+}  // namespace
+
+int igk_sssp(IgExec* ex, const ig_csr* dg, int src, int* d_dist) {
+  const size_t vb = (size_t)dg->nodes * sizeof(int);
+  void *qa, *qb, *fa, *fb, *stamp, *farflag, *hubs;
+  int rc;
+  if ((rc = ig_scratch_get(ex->scratch, IG_SLOT_Q0, vb, &qa))) return rc;
+  if ((rc = ig_scratch_get(ex->scratch, IG_SLOT_Q1, vb, &qb))) return rc;
+  if ((rc = ig_scratch_get(ex->scratch, IG_SLOT_Q2, vb, &fa))) return rc;
+  if ((rc = ig_scratch_get(ex->scratch, IG_SLOT_Q3, vb, &fb))) return rc;
+  if ((rc = ig_scratch_get(ex->scratch, IG_SLOT_V0, vb, &stamp))) return rc;
+  if ((rc = ig_scratch_get(ex->scratch, IG_SLOT_V1, vb, &farflag))) return rc;
+  if ((rc = ig_scratch_get(ex->scratch, IG_SLOT_V2, vb, &hubs))) return rc;
+  if ((rc = ig_exec_reset(ex))) return rc;
+  const IgOptions& o = ig_options();
+  SsspArgs a{dg->nindex, dg->nlist, dg->eweight, dg->nodes, dg->edges, src, d_dist,
+             (int*)qa, (int*)qb, (int*)fa, (int*)fb, (int*)stamp, (int*)farflag, (int*)hubs,
+             ex->d_ctl, ex->timeout_ns, o.hub_degree, o.sssp_delta, o.sssp_delta_scale};
+  void* args[] = {&a};
+  return ig_launch_coop(ex, (const void*)sssp_persistent, kThreads, 0, o.blocks_per_sm, args, nullptr);
+}

@@ -1,0 +1,72 @@
+"""C-ABI checks that need no GPU: the library loads, exports every function
+include/indigo_gb300.h declares, and rejects bad arguments before touching
+the device."""
+import ctypes
+import re
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+HEADER = Path(__file__).resolve().parents[1] / "include" / "indigo_gb300.h"
+
+
+def declared_functions():
+    text = re.sub(r"/\*.*?\*/", "", HEADER.read_text(), flags=re.S)
+    names = re.findall(r"^\s*(?:const\s+)?[\w\s\*]+?\b(ig_\w+)\s*\(", text, flags=re.M)
+    return sorted(set(names))
+
+
+def test_header_parses():
+    names = declared_functions()
+    assert "ig_bfs_vertex" in names and "ig_pr" in names and "ig_tc_vertex" in names
+    assert len(names) > 50
+
+
+def test_every_declared_symbol_is_exported(ig):
+    L = ctypes.CDLL(str(ig.LIB_PATH))
+    missing = [n for n in declared_functions() if not hasattr(L, n)]
+    assert missing == []
+
+
+def test_python_binding_covers_header(ig):
+    from indigo_gb300._lib import SIGNATURES
+    assert sorted(set(declared_functions()) - set(SIGNATURES)) == []
+
+
+def test_version_and_status_strings(ig):
+    L = ig.load()
+    assert L.ig_version() == 1
+    assert L.ig_status_string(0) == b"ok"
+    assert b"sorted" in L.ig_status_string(5)
+    assert L.ig_status_string(999) == b"unknown status"
+
+
+def test_options_roundtrip(ig):
+    old = ig.get_option("bfs_alpha")
+    ig.set_option("bfs_alpha", 20)
+    assert ig.get_option("bfs_alpha") == 20
+    ig.set_option("bfs_alpha", old)
+    with pytest.raises(ig.IndigoError):
+        ig.set_option("no_such_option", 1)
+    with pytest.raises(ig.IndigoError):
+        ig.set_option("blocks_per_sm", 1000)
+
+
+def test_dropins_reject_bad_arguments_without_device(ig):
+    L = ig.load()
+    t = ctypes.c_double()
+    out = np.zeros(4, np.int32)
+    assert L.ig_bfs_vertex(0, None, out.ctypes.data, ctypes.byref(t)) == ig._lib.IG_ERR_INVALID_ARG
+    c = ig.CSR()
+    c.nodes, c.edges = 0, 0
+    assert L.ig_cc_vertex(ctypes.byref(c), out.ctypes.data, ctypes.byref(t)) == ig._lib.IG_ERR_INVALID_ARG
+    g = ig.grid2d(2, 2)
+    hc = g.csr()
+    # source out of range is refused before any device work
+    assert L.ig_bfs_vertex(7, ctypes.byref(hc), out.ctypes.data, ctypes.byref(t)) == ig._lib.IG_ERR_INVALID_ARG
+    assert b"source" in L.ig_last_error()
+    # SSSP needs weights
+    assert L.ig_sssp_vertex(0, ctypes.byref(hc), out.ctypes.data, ctypes.byref(t)) == ig._lib.IG_ERR_INVALID_ARG
+    assert L.ig_pr(None, out.ctypes.data, None, 1e-4, 100, None, None) == ig._lib.IG_ERR_INVALID_ARG
+    assert L.ig_tc_vertex(None, 4, None, None, None) == ig._lib.IG_ERR_INVALID_ARG

@@ -1,0 +1,291 @@
+"""GPU parity: every drop-in entry point (through the C ABI) against the
+oracle and the reference's golden fixtures -- bit-exact for BFS/SSSP/CC/MIS/TC,
+FP32 PageRank within 1e-6 relative L1 of the FP64 oracle run for the same
+number of iterations."""
+import ctypes
+import hashlib
+import math
+
+import numpy as np
+import pytest
+
+from conftest import golden_graphs, kat_graphs
+
+pytestmark = pytest.mark.gpu
+
+INT_MAX = 2147483647
+PR_TOL = 1e-6  # relative L1 against FP64, same iteration count
+
+
+def sha(a):
+    return hashlib.sha256(np.ascontiguousarray(a).tobytes()).hexdigest()
+
+
+@pytest.fixture(scope="module")
+def graphs(ig, gpu):
+    out = {k: v() for k, v in golden_graphs(ig).items()}
+    out.update(kat_graphs(ig))
+    out["rmat14"] = ig.rmat(14, 16, seed=7, maxw=1000)
+    out["road128"] = ig.road(128, 96, 0.05, 0.001, seed=11, maxw=10000)
+    return out
+
+
+def run_all(ig, g, sources):
+    """Runs the six drop-ins on g; returns a dict of host results."""
+    res = {}
+    with ig.DeviceCSR(g) as d:
+        for k, s in enumerate(sources):
+            dist = np.empty(g.nodes, np.int32)
+            ig.GPUbfs_vertex(int(s), d, dist)
+            res[f"bfs{k}"] = dist
+            if g.eweight is not None:
+                dist = np.empty(g.nodes, np.int32)
+                ig.GPUsssp_vertex(int(s), d, dist)
+                res[f"sssp{k}"] = dist
+        lab = np.empty(g.nodes, np.int32)
+        ig.GPUcc_vertex(d, lab)
+        res["cc"] = lab
+        st = np.empty(g.nodes, np.int32)
+        ig.GPUmis_vertex(d, None, st)
+        res["mis"] = st
+        if g.is_sorted():
+            res["tc"] = ig.GPUtc_vertex(g.nodes, d.nindex_ptr, d.nlist_ptr)[0]
+    return res
+
+
+@pytest.mark.parametrize("name", ["grid64", "rmat12", "road64", "er4k", "rmat12_dord"])
+def test_dropins_match_reference_fixtures(ig, golden, graphs, name):
+    _, A = golden
+    g = graphs[name]
+    srcs = A[f"{name}/sources"]
+    r = run_all(ig, g, srcs)
+    for k in range(len(srcs)):
+        assert np.array_equal(r[f"bfs{k}"], A[f"{name}/bfs{k}"]), f"bfs{k}"
+        assert np.array_equal(r[f"sssp{k}"], A[f"{name}/sssp{k}"]), f"sssp{k}"
+    assert np.array_equal(r["cc"], A[f"{name}/cc"])
+    assert np.array_equal(r["mis"], A[f"{name}/mis"].astype(np.int32))
+    assert r["tc"] == int(A[f"{name}/tc"][0])
+
+
+def test_grid256_config_digests(ig, golden, graphs):
+    meta, _ = golden
+    m = meta["digest_only"]["grid256"]
+    g = graphs["grid256"]
+    r = run_all(ig, g, m["sources"])
+    for k in range(len(m["sources"])):
+        assert sha(r[f"bfs{k}"]) == m["sha256"][f"bfs{k}"]
+        assert sha(r[f"sssp{k}"]) == m["sha256"][f"sssp{k}"]
+    assert sha(r["cc"]) == m["sha256"]["cc"]
+    assert sha(r["mis"].astype(np.uint8)) == m["sha256"]["mis"]
+    assert r["tc"] == 0
+
+
+@pytest.mark.parametrize("name", ["single", "two_isolated", "edge", "path", "star", "complete", "two_grids",
+                                  "hubby", "rmat14", "road128"])
+def test_dropins_match_oracle(ig, orc, graphs, name):
+    g = graphs[name]
+    srcs = [0, g.nodes - 1, g.nodes // 2] if g.nodes > 2 else list(range(g.nodes))
+    r = run_all(ig, g, srcs)
+    for k, s in enumerate(srcs):
+        assert np.array_equal(r[f"bfs{k}"], orc.bfs(g, int(s))), f"bfs src {s}"
+        if g.eweight is not None:
+            assert np.array_equal(r[f"sssp{k}"], orc.sssp(g, int(s))), f"sssp src {s}"
+    assert np.array_equal(r["cc"], orc.cc(g))
+    assert np.array_equal(r["mis"], orc.mis(g).astype(np.int32))
+    assert r["tc"] == orc.tc(g)
+
+
+def test_known_answers_on_gpu(ig, graphs):
+    g = ig.grid2d(300, 200)
+    r = run_all(ig, g, [0])
+    y, x = np.divmod(np.arange(g.nodes), 300)
+    assert np.array_equal(r["bfs0"], x + y)
+    assert r["tc"] == 0 and np.all(r["cc"] == 0)
+    k = graphs["complete"]
+    assert run_all(ig, k, [0])["tc"] == math.comb(k.nodes, 3)
+
+
+def test_unreachable_is_int_max(ig, graphs):
+    g = graphs["two_grids"]
+    r = run_all(ig, g, [0])
+    assert np.all(r["bfs0"][100:] == INT_MAX) and np.all(r["sssp0"][100:] == INT_MAX)
+    assert np.all(r["bfs0"][:100] < INT_MAX)
+
+
+@pytest.mark.parametrize("name", ["grid64", "rmat12", "er4k", "rmat14", "hubby", "star"])
+def test_pagerank_fp32_against_fp64(ig, orc, graphs, name):
+    g = graphs[name]
+    deg = g.degree()
+    scores = np.full(g.nodes, np.float32(1.0) / np.float32(g.nodes), np.float32)
+    it, _ = ig.PR_GPU(g, scores, deg, epsilon=1e-6, max_iter=100)
+    ref, it64, _ = orc.pr_f64(g, iters=it)
+    assert it64 == it
+    rel_l1 = np.abs(scores.astype(np.float64) - ref).sum() / np.abs(ref).sum()
+    assert rel_l1 <= PR_TOL, rel_l1
+    # iteration count agrees with the reference FP32 algorithm to within one,
+    # unless the uncompensated FP32 sum never gets below epsilon (it then
+    # stops at max_iter, e.g. on the bipartite star, while Kahan converges)
+    _, it32, _ = orc.pr_f32(g, 1e-6, 100)
+    assert abs(it32 - it) <= 1 or (it32 == 100 and it < 100)
+
+
+def test_pagerank_reference_constants(ig, orc, golden, graphs):
+    """EPSILON 1e-4 / MAX_ITER 100 as in include/pr_cuda.h: same iteration
+    count as the reference program and scores within tolerance of it."""
+    _, A = golden
+    g = graphs["rmat12"]
+    scores = np.full(g.nodes, np.float32(1.0) / np.float32(g.nodes), np.float32)
+    it, _ = ig.PR_GPU(g, scores, g.degree())
+    _, it_ref, _ = orc.pr_f32(g, 1e-4, 100)
+    assert abs(it - it_ref) <= 1
+    ref = A["rmat12/pr"].astype(np.float64)
+    assert np.abs(scores - ref).sum() / ref.sum() < 1e-5
+
+
+def test_pagerank_deterministic(ig, graphs):
+    g = graphs["rmat14"]
+    outs = []
+    for _ in range(2):
+        s = np.full(g.nodes, np.float32(1.0) / np.float32(g.nodes), np.float32)
+        ig.PR_GPU(g, s, g.degree(), 1e-6, 100)
+        outs.append(s)
+    assert np.array_equal(outs[0], outs[1])
+
+
+def test_pagerank_hub_split_path(ig, orc, graphs):
+    """Forces the chunked hub path (hub degree 64, chunks of 32 edges)."""
+    g = graphs["rmat14"]
+    old = (ig.get_option("pr_hub_degree"), ig.get_option("pr_chunk"))
+    try:
+        ig.set_option("pr_hub_degree", 64)
+        ig.set_option("pr_chunk", 32)
+        s = np.full(g.nodes, np.float32(1.0) / np.float32(g.nodes), np.float32)
+        it, _ = ig.PR_GPU(g, s, g.degree(), 1e-6, 100)
+    finally:
+        ig.set_option("pr_hub_degree", old[0])
+        ig.set_option("pr_chunk", old[1])
+    ref, _, _ = orc.pr_f64(g, iters=it)
+    assert np.abs(s - ref).sum() / ref.sum() <= PR_TOL
+
+
+def test_hub_paths_forced(ig, orc, graphs):
+    """Small hub degree sends many vertices through the grid-wide hub
+    expansion of BFS / SSSP / CC."""
+    g = graphs["rmat14"]
+    old = ig.get_option("hub_degree")
+    try:
+        ig.set_option("hub_degree", 32)
+        r = run_all(ig, g, [0, 5])
+    finally:
+        ig.set_option("hub_degree", old)
+    for k, s in enumerate([0, 5]):
+        assert np.array_equal(r[f"bfs{k}"], orc.bfs(g, s))
+        assert np.array_equal(r[f"sssp{k}"], orc.sssp(g, s))
+    assert np.array_equal(r["cc"], orc.cc(g))
+
+
+@pytest.mark.parametrize("alpha,beta", [(1, 1), (1000000, 24), (2, 1000000)])
+def test_bfs_direction_settings(ig, orc, graphs, alpha, beta):
+    g = graphs["rmat14"]
+    old = (ig.get_option("bfs_alpha"), ig.get_option("bfs_beta"))
+    try:
+        ig.set_option("bfs_alpha", alpha)
+        ig.set_option("bfs_beta", beta)
+        r = run_all(ig, g, [3])
+    finally:
+        ig.set_option("bfs_alpha", old[0])
+        ig.set_option("bfs_beta", old[1])
+    assert np.array_equal(r["bfs0"], orc.bfs(g, 3))
+
+
+@pytest.mark.parametrize("delta", [1, 7, 1000, 100000000])
+def test_sssp_bucket_widths(ig, orc, graphs, delta):
+    g = graphs["road128"]
+    old = ig.get_option("sssp_delta")
+    try:
+        ig.set_option("sssp_delta", delta)
+        r = run_all(ig, g, [0])
+    finally:
+        ig.set_option("sssp_delta", old)
+    assert np.array_equal(r["sssp0"], orc.sssp(g, 0))
+
+
+def test_edge_forms_equal_vertex_forms(ig, graphs):
+    g = graphs["rmat12"]
+    sp = g.sp()
+    with ig.DeviceCSR(g) as d:
+        a = np.empty(g.nodes, np.int32)
+        b = np.empty(g.nodes, np.int32)
+        ig.GPUbfs_vertex(5, d, a)
+        ig.GPUbfs_edge(5, d, b, sp)
+        assert np.array_equal(a, b)
+        ig.GPUsssp_vertex(5, d, a)
+        ig.GPUsssp_edge(5, d, b, sp)
+        assert np.array_equal(a, b)
+        ig.GPUcc_vertex(d, a)
+        ig.GPUcc_edge(d, b, sp)
+        assert np.array_equal(a, b)
+
+
+def test_device_api_matches_dropins(ig, graphs):
+    g = graphs["rmat14"]
+    r = run_all(ig, g, [7])
+    with ig.DeviceCSR(g) as d:
+        dg = ig.DeviceGraph(d)
+        buf = ig.DeviceBuffer(4 * g.nodes)
+        dg.bfs(7, buf)
+        assert dg.last_run().status == 0
+        assert np.array_equal(buf.to_array(np.int32, g.nodes), r["bfs0"])
+        dg.sssp(7, buf)
+        assert np.array_equal(buf.to_array(np.int32, g.nodes), r["sssp0"])
+        dg.cc(buf)
+        assert np.array_equal(buf.to_array(np.int32, g.nodes), r["cc"])
+        dg.mis(buf)
+        assert np.array_equal(buf.to_array(np.int32, g.nodes), r["mis"])
+        cnt = ig.DeviceBuffer(8)
+        dg.tc(cnt)
+        assert int(cnt.to_array(np.uint64, 1)[0]) == r["tc"]
+        sc = ig.DeviceBuffer.from_array(np.full(g.nodes, np.float32(1.0) / np.float32(g.nodes), np.float32))
+        dg.pagerank(sc, 1e-6, 100)
+        info = dg.last_run()
+        assert info.status == 0 and info.iterations > 1 and info.residual < 1e-6
+        dg.close()
+
+
+def test_tc_rejects_unsorted(ig, graphs):
+    g = graphs["grid64"]
+    nl = g.nlist.copy()
+    nl[0], nl[1] = nl[1], nl[0]
+    bad = ig.Graph(g.nindex, nl)
+    with ig.DeviceCSR(bad) as d:
+        with pytest.raises(ig.IndigoError) as e:
+            ig.GPUtc_vertex(bad.nodes, d.nindex_ptr, d.nlist_ptr)
+        assert e.value.status == ig._lib.IG_ERR_UNSORTED
+        # the context stays usable after the error
+        dist = np.empty(bad.nodes, np.int32)
+        ig.GPUbfs_vertex(0, d, dist)
+        assert dist[0] == 0
+
+
+def test_bounded_wait_reports_timeout(ig, graphs):
+    """A grid barrier that one block never reaches ends in IG_ERR_TIMEOUT
+    after the bound, and the device keeps working afterwards."""
+    L = ig.load()
+    st = ctypes.c_int(-1)
+    ig.check(L.ig_selftest_wait_timeout(200, ctypes.byref(st)))
+    assert st.value == ig._lib.IG_ERR_TIMEOUT
+    g = graphs["grid64"]
+    with ig.DeviceCSR(g) as d:
+        dist = np.empty(g.nodes, np.int32)
+        ig.GPUbfs_vertex(0, d, dist)
+        assert dist.max() == 126
+
+
+def test_repeated_calls_reuse_scratch(ig, orc, graphs):
+    """Alternating graph sizes exercise the grow-only scratch pool."""
+    for name in ["rmat14", "grid64", "rmat14", "path"]:
+        g = graphs[name]
+        with ig.DeviceCSR(g) as d:
+            dist = np.empty(g.nodes, np.int32)
+            ig.GPUbfs_vertex(0, d, dist)
+            assert np.array_equal(dist, orc.bfs(g, 0))
