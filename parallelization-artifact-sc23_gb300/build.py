@@ -76,5 +76,44 @@ def build(force: bool = False, verbose: bool = False) -> Path:
     return LIB
 
 
+SHIM = PKG / "shim"
+SHIMS = ["bfs_vertex", "sssp_vertex", "cc_vertex", "mis_vertex", "pr", "tc_vertex",
+         "bfs_edge", "sssp_edge", "cc_edge", "mis_edge", "tc_edge"]
+
+
+def build_shims(reference_include: str, verbose: bool = False) -> list:
+    """Compiles the drop-in translation units of shim/ with the reference's
+    own driver headers (include/*_cuda.h, unmodified) into _build/shim/, each
+    linked against the library.  The result is the reference's driver program
+    (its main, timer and verifier) running the GB300 kernels."""
+    inc = Path(reference_include)
+    if not (inc / "ECLgraph.h").exists():
+        return []
+    lib = build()
+    out = OBJ / "shim"
+    out.mkdir(parents=True, exist_ok=True)
+
+    def one(name):
+        exe = out / name
+        src = SHIM / f"{name}_gb300.cu"
+        if exe.exists() and exe.stat().st_mtime >= max(src.stat().st_mtime, lib.stat().st_mtime):
+            return exe
+        cmd = [_nvcc(), "-O3", "-std=c++17", *ARCH, "-w", "-include", str(SHIM / "compat_cuda13.h"),
+               "-I", str(inc), "-I", str(INCLUDE), "-I", str(SHIM), str(src), "-o", str(exe),
+               "-L", str(lib.parent), "-lindigo_gb300", "-Xlinker", "-rpath", "-Xlinker", str(lib.parent)]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"shim build failed: {' '.join(cmd)}\n{r.stderr}")
+        return exe
+
+    with cf.ThreadPoolExecutor(max_workers=min(8, os.cpu_count() or 4)) as ex:
+        exes = list(ex.map(one, SHIMS))
+    if verbose:
+        print(f"built {len(exes)} drop-in driver programs in {out}")
+    return exes
+
+
 if __name__ == "__main__":
     build(force="--force" in sys.argv, verbose=True)
+    ref = os.environ.get("INDIGO_REFERENCE", "/root/reference")
+    build_shims(os.path.join(ref, "include"), verbose=True)

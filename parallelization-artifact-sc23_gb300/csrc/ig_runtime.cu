@@ -283,7 +283,8 @@ extern "C" int ig_csr_free_device(ig_csr* d) {
 }
 extern "C" int ig_stream_create(void** s) {
   if (!s) return ig_fail(IG_ERR_INVALID_ARG, "null");
-  IG_CU(cudaStreamCreateWithFlags((cudaStream_t*)s, cudaStreamNonBlocking));
+  // blocking stream: ordered with legacy-default-stream copies such as ig_memcpy
+  IG_CU(cudaStreamCreate((cudaStream_t*)s));
   return IG_OK;
 }
 extern "C" int ig_stream_destroy(void* s) {
@@ -524,7 +525,9 @@ extern "C" int ig_graph_create(const ig_csr* d_g, ig_graph** out) {
   h->g = *d_g;
   IG_CU(cudaGetDevice(&h->device));
   IG_CU(cudaDeviceGetAttribute(&h->sms, cudaDevAttrMultiProcessorCount, h->device));
-  IG_CU(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
+  // a blocking stream, so ig_memcpy (legacy default stream) of a result waits
+  // for the graph's queued work
+  IG_CU(cudaStreamCreate(&h->stream));
   IG_CU(cudaMallocHost((void**)&h->h_ctl, sizeof(IgCtl)));
   memset(h->h_ctl, 0, sizeof(IgCtl));
   h->scratch.device = h->device;

@@ -9,13 +9,14 @@
 //
 // GB300 formulation (same count, far less work on skewed graphs):
 //   1. check  : adjacency strictly increasing and no self loop
-//   2. orient : keep edge u->w iff (deg u, u) < (deg w, w), so every vertex
-//               keeps at most O(sqrt E) out-neighbours; the kept lists stay
-//               sorted by id; counted per vertex, scanned, then filled
-//   3. count  : for every u, the warp stages N+(u) in shared memory (when it
-//               fits) and, with the load-balanced warp expansion over the
-//               lists N+(v) of u's out-neighbours v, binary-searches every
-//               w in N+(v) inside N+(u); a hit is the triangle {u, v, w}.
+//   2. orient : edge u->w iff (deg u, u) < (deg w, w), so every vertex keeps
+//               O(sqrt E) out-neighbours N+; each list is split into its out
+//               part (id order) and its in part N-; counted, scanned, filled
+//   3. count  : work item = (middle vertex v, <= kChunk in-neighbours u of
+//               v).  The warp hashes N+(v) into shared memory and probes
+//               every w of the out-lists N+(u) (load-balanced warp
+//               expansion); a hit is the triangle u -> v -> w, counted once
+//               (at its middle vertex).  Work: sum over u of |N+(u)|^2 probes.
 #include "ig_device.cuh"
 #include "ig_options.h"
 
@@ -23,13 +24,15 @@ namespace {
 
 constexpr int kThreads = 256;
 constexpr int kWarps = kThreads / 32;
-constexpr int kStage = 1024;  // out-neighbours of u staged per warp
+constexpr int kChunk = 64;      // in-neighbours per work item
+constexpr int kOrientHub = 256; // lists longer than this are split by one block each
+constexpr int kHashCap = 2048;  // hash slots per warp (out-degree <= 1024 is hashed)
 
 __device__ __forceinline__ bool before(int du, int u, int dw, int w) { return du < dw || (du == dw && u < w); }
 
 __global__ void __launch_bounds__(kThreads) tc_orient_count(const int* __restrict__ nindex,
                                                             const int* __restrict__ nlist, int n, int* out_cnt,
-                                                            IgCtl* ctl) {
+                                                            int* item_cnt, int* hubs, IgCtl* ctl) {
   using namespace ig;
   __shared__ int s_cnt[kWarps][32];
   const int lane = lane_id(), wib = threadIdx.x >> 5;
@@ -45,8 +48,10 @@ __global__ void __launch_bounds__(kThreads) tc_orient_count(const int* __restric
     s_cnt[wib][lane] = 0;
     __syncwarp();
     const int vv = (int)v;
+    const bool hub = deg > kOrientHub;  // counted by one block each in tc_orient_hubs
+    warp_append(hub, vv, hubs, &ctl->i32[0], n, ctl);
     bool bad = false;
-    warp_expand(beg, deg, [&](bool act, int e, int j) {
+    warp_expand(beg, hub ? 0 : deg, [&](bool act, int e, int j) {
       const int u = __shfl_sync(IG_FULL, vv, j);
       const int du = __shfl_sync(IG_FULL, deg, j);
       const int ub = __shfl_sync(IG_FULL, beg, j);
@@ -61,17 +66,25 @@ __global__ void __launch_bounds__(kThreads) tc_orient_count(const int* __restric
     });
     __syncwarp();
     if (bad) raise(ctl, IG_ERR_UNSORTED);
-    if (v < n) out_cnt[v] = s_cnt[wib][lane];
+    if (v < n && !hub) {
+      const int oc = s_cnt[wib][lane];
+      out_cnt[v] = oc;
+      // work items of middle vertex v: its in-neighbours in chunks of kChunk
+      item_cnt[v] = oc > 0 ? (deg - oc + kChunk - 1) / kChunk : 0;
+    }
     __syncwarp();
   }
 }
 
+// Splits every adjacency list into its out part (kept in id order) and its
+// in part (in_off[v] = nindex[v] - out_off[v]).
 __global__ void __launch_bounds__(kThreads) tc_orient_fill(const int* __restrict__ nindex,
                                                            const int* __restrict__ nlist, int n,
                                                            const int* __restrict__ out_off, int* out_list,
-                                                           const IgCtl* ctl) {
+                                                           int* in_list, const IgCtl* ctl) {
   using namespace ig;
   __shared__ int s_pos[kWarps][32];
+  __shared__ int s_ipos[kWarps][32];
   if (ctl->err) return;
   const int lane = lane_id(), wib = threadIdx.x >> 5;
   const long long gtid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -82,11 +95,13 @@ __global__ void __launch_bounds__(kThreads) tc_orient_fill(const int* __restrict
     if (v < n) {
       beg = __ldg(&nindex[v]);
       deg = __ldg(&nindex[v + 1]) - beg;
-      s_pos[wib][lane] = out_off[v];
+      const int oo = out_off[v];
+      s_pos[wib][lane] = oo;
+      s_ipos[wib][lane] = beg - oo;
     }
     __syncwarp();
     const int vv = (int)v;
-    warp_expand(beg, deg, [&](bool act, int e, int j) {
+    warp_expand(beg, deg > kOrientHub ? 0 : deg, [&](bool act, int e, int j) {
       const int u = __shfl_sync(IG_FULL, vv, j);
       const int du = __shfl_sync(IG_FULL, deg, j);
       bool keep = false;
@@ -99,13 +114,81 @@ __global__ void __launch_bounds__(kThreads) tc_orient_fill(const int* __restrict
       // order-preserving compaction among lanes with the same owner
       const unsigned same = __match_any_sync(IG_FULL, act ? j : -1);
       const unsigned km = __ballot_sync(IG_FULL, keep) & same;
+      const unsigned im = __ballot_sync(IG_FULL, act && !keep) & same;
       if (keep) out_list[s_pos[wib][j] + __popc(km & lanemask_lt())] = w;
+      else if (act) in_list[s_ipos[wib][j] + __popc(im & lanemask_lt())] = w;
       __syncwarp();
-      const int leader = 31 - __clz(same);  // highest lane of the group updates the cursor
-      if (act && lane == leader) s_pos[wib][j] += __popc(km);
+      const int leader = 31 - __clz(same);  // highest lane of the group advances the cursors
+      if (act && lane == leader) {
+        s_pos[wib][j] += __popc(km);
+        s_ipos[wib][j] += __popc(im);
+      }
       __syncwarp();
     });
     __syncwarp();
+  }
+}
+
+// Vertices above kOrientHub neighbours, one block each: count (and check)
+// their out-neighbours.
+__global__ void __launch_bounds__(kThreads) tc_orient_hubs_count(const int* __restrict__ nindex,
+                                                                 const int* __restrict__ nlist, int n,
+                                                                 const int* hubs, int* out_cnt, int* item_cnt,
+                                                                 IgCtl* ctl) {
+  using namespace ig;
+  __shared__ int s_tmp[33];
+  const int nh = ctl->i32[0];
+  for (int h = blockIdx.x; h < nh; h += gridDim.x) {
+    const int u = hubs[h];
+    const int b = __ldg(&nindex[u]), e = __ldg(&nindex[u + 1]), du = e - b;
+    int keep = 0;
+    bool bad = false;
+    for (int k = b + threadIdx.x; k < e; k += blockDim.x) {
+      const int w = __ldg(&nlist[k]);
+      if (w == u || (k > b && __ldg(&nlist[k - 1]) >= w) || w < 0 || w >= n) bad = true;
+      else if (before(du, u, __ldg(&nindex[w + 1]) - __ldg(&nindex[w]), w)) keep++;
+    }
+    if (bad) raise(ctl, IG_ERR_UNSORTED);
+    int total;
+    block_scan_int(keep, s_tmp, &total);
+    if (threadIdx.x == 0) {
+      out_cnt[u] = total;
+      item_cnt[u] = total > 0 ? (du - total + kChunk - 1) / kChunk : 0;
+    }
+    __syncthreads();
+  }
+}
+
+// Order-preserving split of the hub lists into out and in parts, one block per hub.
+__global__ void __launch_bounds__(kThreads) tc_orient_hubs_fill(const int* __restrict__ nindex,
+                                                                const int* __restrict__ nlist, const int* hubs,
+                                                                const int* __restrict__ out_off, int* out_list,
+                                                                int* in_list, const IgCtl* ctl) {
+  using namespace ig;
+  __shared__ int s_tmp[33];
+  if (ctl->err) return;
+  const int nh = ctl->i32[0];
+  for (int h = blockIdx.x; h < nh; h += gridDim.x) {
+    const int u = hubs[h];
+    const int b = __ldg(&nindex[u]), e = __ldg(&nindex[u + 1]), du = e - b;
+    int op = out_off[u], ip = b - op;
+    for (int t = b; t < e; t += blockDim.x) {
+      const int k = t + threadIdx.x;
+      int w = 0;
+      bool act = k < e, keep = false;
+      if (act) {
+        w = __ldg(&nlist[k]);
+        keep = before(du, u, __ldg(&nindex[w + 1]) - __ldg(&nindex[w]), w);
+      }
+      int tk, ti;
+      const int pk = block_scan_int(keep ? 1 : 0, s_tmp, &tk);
+      const int pi = block_scan_int(act && !keep ? 1 : 0, s_tmp, &ti);
+      if (keep) out_list[op + pk] = w;
+      else if (act) in_list[ip + pi] = w;
+      op += tk;
+      ip += ti;
+    }
+    __syncthreads();
   }
 }
 
@@ -120,38 +203,87 @@ __device__ __forceinline__ bool contains(const int* list, int len, int x) {
   return lo < len && list[lo] == x;
 }
 
+__device__ __forceinline__ unsigned hash_slot(int w, unsigned mask) { return ((unsigned)w * 0x9E3779B1u >> 7) & mask; }
+
+// One work item = (middle vertex v, a chunk of kChunk of its in-neighbours u).
+// The warp hashes N+(v) into its shared-memory table, then walks the
+// out-lists N+(u) of the chunk's in-neighbours (load-balanced) and probes:
+// w in N+(u) and in N+(v) closes the triangle u -> v -> w, counted once at v.
 __global__ void __launch_bounds__(kThreads) tc_count(const int* __restrict__ out_off, const int* __restrict__ out_list,
-                                                     int n, unsigned long long* count, const IgCtl* ctl) {
+                                                     const int* __restrict__ nindex, const int* __restrict__ in_list,
+                                                     const int* __restrict__ item_off, int n,
+                                                     unsigned long long* count, const IgCtl* ctl) {
   using namespace ig;
-  __shared__ int s_list[kWarps][kStage];
+  extern __shared__ int s_tab[];
   if (ctl->err) return;
   const int lane = lane_id(), wib = threadIdx.x >> 5;
+  int* tab = s_tab + wib * kHashCap;
   const int warp_g = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int nwarps = (gridDim.x * blockDim.x) >> 5;
+  const int items = __ldg(&item_off[n]);
   unsigned long long local = 0;
-  for (int u = warp_g; u < n; u += nwarps) {
-    const int ub = __ldg(&out_off[u]), ue = __ldg(&out_off[u + 1]);
-    const int ulen = ue - ub;
-    if (ulen < 2) continue;
-    const int* ulist = out_list + ub;
-    const bool staged = ulen <= kStage;
-    if (staged) {
-      for (int k = lane; k < ulen; k += 32) s_list[wib][k] = __ldg(&out_list[ub + k]);
-      __syncwarp();
-      ulist = s_list[wib];
+  int cur_v = -1;
+  unsigned mask = 0;
+  bool hashed = false;
+  for (int it = warp_g; it < items; it += nwarps) {
+    // middle vertex: largest v with item_off[v] <= it
+    int lo = 0, hi = n - 1;
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (__ldg(&item_off[mid]) <= it) lo = mid;
+      else hi = mid - 1;
     }
-    for (int g = 0; g < ulen; g += 32) {
-      int vb = 0, vd = 0;
-      if (g + lane < ulen) {
-        const int v = staged ? s_list[wib][g + lane] : __ldg(&out_list[ub + g + lane]);
-        vb = __ldg(&out_off[v]);
-        vd = __ldg(&out_off[v + 1]) - vb;
+    const int v = lo;
+    const int vb = __ldg(&out_off[v]);
+    const int vd = __ldg(&out_off[v + 1]) - vb;
+    if (v != cur_v) {
+      cur_v = v;
+      hashed = 2 * vd <= kHashCap;
+      if (hashed) {
+        int cap = 32;
+        while (cap < 2 * vd) cap <<= 1;
+        mask = (unsigned)cap - 1;
+        __syncwarp();
+        for (int k = lane; k < cap; k += 32) tab[k] = -1;
+        __syncwarp();
+        for (int k = lane; k < vd; k += 32) {
+          const int w = __ldg(&out_list[vb + k]);
+          unsigned h = hash_slot(w, mask);
+          while (atomicCAS(&tab[h], -1, w) != -1) h = (h + 1) & mask;
+        }
+        __syncwarp();
       }
-      warp_expand(vb, vd, [&](bool act, int e, int) {
-        if (act && contains(ulist, ulen, __ldg(&out_list[e]))) local++;
+    }
+    const int ib = __ldg(&nindex[v]) - vb;  // in_off[v]
+    const int iend = __ldg(&nindex[v + 1]) - __ldg(&out_off[v + 1]);
+    const int c0 = ib + (it - __ldg(&item_off[v])) * kChunk;
+    const int c1 = min(c0 + kChunk, iend);
+    for (int g = c0; g < c1; g += 32) {
+      int ub = 0, ud = 0;
+      if (g + lane < c1) {
+        const int u = __ldg(&in_list[g + lane]);
+        ub = __ldg(&out_off[u]);
+        ud = __ldg(&out_off[u + 1]) - ub;
+      }
+      warp_expand(ub, ud, [&](bool act, int e, int) {
+        if (!act) return;
+        const int w = __ldg(&out_list[e]);
+        if (hashed) {
+          unsigned h = hash_slot(w, mask);
+          while (true) {
+            const int t = tab[h];
+            if (t == w) {
+              local++;
+              break;
+            }
+            if (t == -1) break;
+            h = (h + 1) & mask;
+          }
+        } else if (contains(out_list + vb, vd, w)) {
+          local++;
+        }
       });
     }
-    __syncwarp();
   }
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) local += __shfl_xor_sync(IG_FULL, local, o);
@@ -162,20 +294,43 @@ __global__ void __launch_bounds__(kThreads) tc_count(const int* __restrict__ out
 
 int igk_tc(IgExec* ex, int nodes, int edges, const int* d_nindex, const int* d_nlist, unsigned long long* d_count) {
   const size_t vb = ((size_t)nodes + 1) * sizeof(int);
-  void *cnt, *off, *list;
+  void *cnt, *off, *icnt, *ioff, *list, *inl, *hubs;
   int rc;
   if ((rc = ig_scratch_get(ex->scratch, IG_SLOT_V0, vb, &cnt))) return rc;
   if ((rc = ig_scratch_get(ex->scratch, IG_SLOT_V1, vb, &off))) return rc;
+  if ((rc = ig_scratch_get(ex->scratch, IG_SLOT_V2, vb, &icnt))) return rc;
+  if ((rc = ig_scratch_get(ex->scratch, IG_SLOT_Q0, vb, &ioff))) return rc;
+  if ((rc = ig_scratch_get(ex->scratch, IG_SLOT_Q1, vb, &hubs))) return rc;
   if ((rc = ig_scratch_get(ex->scratch, IG_SLOT_E0, std::max<size_t>(1, (size_t)edges) * sizeof(int), &list)))
+    return rc;
+  if ((rc = ig_scratch_get(ex->scratch, IG_SLOT_G1, std::max<size_t>(1, (size_t)edges) * sizeof(int), &inl)))
     return rc;
   if ((rc = ig_exec_reset(ex))) return rc;
   if ((rc = ig_cuda_check((int)cudaMemsetAsync(d_count, 0, sizeof(unsigned long long), ex->stream), "memset")))
     return rc;
+  static bool attr_set[64] = {};
+  const size_t smem = (size_t)kWarps * kHashCap * sizeof(int);
+  if (ex->device >= 0 && ex->device < 64 && !attr_set[ex->device]) {
+    if ((rc = ig_cuda_check((int)cudaFuncSetAttribute((const void*)tc_count,
+                                                      cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
+                            "tc smem attribute")))
+      return rc;
+    attr_set[ex->device] = true;
+  }
   const int grid = std::max(1, std::min((nodes + kThreads - 1) / kThreads, ex->sms * 8));
-  tc_orient_count<<<grid, kThreads, 0, ex->stream>>>(d_nindex, d_nlist, nodes, (int*)cnt, ex->d_ctl);
+  tc_orient_count<<<grid, kThreads, 0, ex->stream>>>(d_nindex, d_nlist, nodes, (int*)cnt, (int*)icnt, (int*)hubs,
+                                                      ex->d_ctl);
+  tc_orient_hubs_count<<<ex->sms * 8, kThreads, 0, ex->stream>>>(d_nindex, d_nlist, nodes, (const int*)hubs,
+                                                                 (int*)cnt, (int*)icnt, ex->d_ctl);
   if ((rc = igk_exclusive_scan(ex, (const int*)cnt, (int*)off, nodes, nullptr))) return rc;
-  tc_orient_fill<<<grid, kThreads, 0, ex->stream>>>(d_nindex, d_nlist, nodes, (const int*)off, (int*)list, ex->d_ctl);
-  tc_count<<<ex->sms * 8, kThreads, 0, ex->stream>>>((const int*)off, (const int*)list, nodes, d_count, ex->d_ctl);
-  ig_count_launches(3);
+  if ((rc = igk_exclusive_scan(ex, (const int*)icnt, (int*)ioff, nodes, nullptr))) return rc;
+  tc_orient_fill<<<grid, kThreads, 0, ex->stream>>>(d_nindex, d_nlist, nodes, (const int*)off, (int*)list,
+                                                     (int*)inl, ex->d_ctl);
+  tc_orient_hubs_fill<<<ex->sms * 8, kThreads, 0, ex->stream>>>(d_nindex, d_nlist, (const int*)hubs,
+                                                                (const int*)off, (int*)list, (int*)inl, ex->d_ctl);
+  tc_count<<<ex->sms * 3, kThreads, smem, ex->stream>>>((const int*)off, (const int*)list, d_nindex,
+                                                        (const int*)inl, (const int*)ioff, nodes, d_count,
+                                                        ex->d_ctl);
+  ig_count_launches(5);
   return ig_cuda_check((int)cudaGetLastError(), "tc launch");
 }

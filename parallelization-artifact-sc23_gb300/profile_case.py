@@ -4,6 +4,7 @@ directed edges, so the 250 MB neighbour list exceeds the 129 MB L2), run a
 few times through the device-resident API.
 
     python parallelization-artifact-sc23_gb300/profile_case.py --algo bfs [--scale 21] [--repeat 3]
+           [--opt sssp_delta=100 ...]
 
 It prints one line per run with the CUDA-event time and the algorithmic
 bytes, so a capture can be related to the bench's roofline figures."""
@@ -25,7 +26,11 @@ def main():
     ap.add_argument("--algo", choices=["bfs", "sssp", "cc", "mis", "pr", "tc"], required=True)
     ap.add_argument("--scale", type=int, default=21)
     ap.add_argument("--repeat", type=int, default=3)
+    ap.add_argument("--opt", action="append", default=[], help="kernel option name=value (ig_set_option)")
     args = ap.parse_args()
+    for o in args.opt:
+        name, value = o.split("=")
+        ig.set_option(name, int(value))
     g = ig.rmat(args.scale, 16, seed=7, maxw=1000)
     if args.algo == "tc":
         g = g.degree_ordered()
@@ -61,7 +66,7 @@ def main():
             ig.check(info.status)
             mult = max(1, info.iterations) if args.algo == "pr" else 1
             gbs = bytes_per[args.algo] * mult / (ms * 1e-3) / 1e9
-            print(f"{args.algo} run {r}: {ms:.3f} ms, iterations {info.iterations}, "
+            print(f"{args.algo} run {r}: {ms:.3f} ms, iterations {info.iterations}, work {info.work}, "
                   f"{E / (ms * 1e-3) / 1e9:.2f} GTEPS, {gbs:.0f} GB/s algorithmic (V={V}, E={E})")
         G.close()
 
