@@ -194,6 +194,20 @@ int ig_mis_edge(const ig_csr* d_g, const int* d_sp, unsigned int* h_priority,
 int ig_tc_edge(long long* count, int edges, const int* d_nindex, const int* d_nlist,
                const int* d_sp, double* seconds);
 
+/* No counterpart in the reference.  BFS for callers that cannot allocate
+ * device memory (a host framework owns the memory budget, or the call sits
+ * where the allocator must not be touched): the caller passes the device
+ * graph (d_g, device nindex/nlist) and the device output d_dist[nodes]; the
+ * kernel's scratch is a fixed array inside the library's device image
+ * (12 MiB per GPU, held until exit), so graphs are limited to 1,048,576
+ * vertices (IG_ERR_INVALID_ARG beyond).  Runs on `stream` (NULL: legacy
+ * default) and returns when the result is complete.  No cudaMalloc or
+ * cudaFree is made.  The first call on a device resolves the array's address
+ * with cudaGetSymbolAddress: make it before any stream capture.  Calls share
+ * the array, so calls whose GPU work overlaps race; order them.  Results are
+ * identical to ig_bfs_vertex. */
+int ig_bfs_vertex_noalloc(int src, const ig_csr* d_g, int* d_dist, void* stream);
+
 /* ---------------------------------------------------------------------------
  * Device-resident API: a graph already in HBM, results written to device
  * buffers, asynchronous on the graph's stream.  Scratch is allocated once

@@ -166,3 +166,25 @@ int igk_bfs(IgExec* ex, const ig_csr* dg, int src, int* d_dist) {
   void* args[] = {&a};
   return ig_launch_coop(ex, (const void*)bfs_persistent, kThreads, 0, o.blocks_per_sm, args, nullptr);
 }
+
+// Launch on caller-provided scratch (two queues and a hub list of `nodes`
+// ints each, and the control block already in ex->d_ctl).  Allocates nothing
+// and keeps no host-side cache: the occupancy query and the cooperative
+// launch are the only runtime calls.
+int igk_bfs_launch_prealloc(IgExec* ex, const ig_csr* dg, int src, int* d_dist, int* qa, int* qb, int* hubs) {
+  int per_sm = 0;
+  int rc = ig_cuda_check((int)cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, bfs_persistent, kThreads, 0),
+                         "occupancy");
+  if (rc) return rc;
+  const IgOptions& o = ig_options();
+  if (o.blocks_per_sm > 0) per_sm = std::min(per_sm, o.blocks_per_sm);
+  if (per_sm < 1) return ig_fail(IG_ERR_CUDA, "persistent kernel cannot be resident (occupancy 0)");
+  BfsArgs a{dg->nindex, dg->nlist, dg->nodes, dg->edges, src, d_dist, qa, qb, hubs,
+            ex->d_ctl, ex->timeout_ns, o.hub_degree, o.bfs_alpha, o.bfs_beta};
+  void* args[] = {&a};
+  rc = ig_cuda_check((int)cudaLaunchCooperativeKernel((const void*)bfs_persistent, dim3(per_sm * ex->sms),
+                                                      dim3(kThreads), args, 0, ex->stream),
+                     "cooperative launch");
+  if (rc == IG_OK) ig_count_launches(1);
+  return rc;
+}

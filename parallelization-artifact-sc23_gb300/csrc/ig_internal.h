@@ -120,6 +120,7 @@ void ig_count_launches(int n);
 // Algorithm launchers (enqueue on ex->stream; errors surface in ig_exec_finish)
 // ---------------------------------------------------------------------------
 int igk_bfs(IgExec* ex, const ig_csr* dg, int src, int* d_dist);
+int igk_bfs_launch_prealloc(IgExec* ex, const ig_csr* dg, int src, int* d_dist, int* qa, int* qb, int* hubs);
 int igk_sssp(IgExec* ex, const ig_csr* dg, int src, int* d_dist);
 int igk_cc(IgExec* ex, const ig_csr* dg, int* d_label);
 int igk_mis(IgExec* ex, const ig_csr* dg, int* d_status, unsigned int* d_prio);

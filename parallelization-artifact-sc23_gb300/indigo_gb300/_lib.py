@@ -123,6 +123,7 @@ SIGNATURES = {
     "ig_selftest_wait_timeout": (_I, [_I, _PI]),
     "ig_graph_set_stream": (_I, [_P, _P]),
     "ig_kernel_launches": (_I, [ctypes.POINTER(ctypes.c_longlong)]),
+    "ig_bfs_vertex_noalloc": (_I, [_I, _PCSR, _P, _P]),
 }
 
 _lib = None
