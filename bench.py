@@ -393,9 +393,8 @@ def validate(ig, g, G, GT, sources, dist_buf, lab, st, scores, count) -> dict:
     for _ in range(2):
         x = (((x >> np.uint64(16)) ^ x) * np.uint64(0x45D9F3B)) & np.uint64(0xFFFFFFFF)
     pr = ((x >> np.uint64(16)) ^ x).astype(np.int64)
-    key = pr * (1 << 32) + np.arange(V, dtype=np.int64)  # (priority, id) order
     inset = ms == 1
-    larger = key[nl] > key[src]
+    larger = (pr[nl] > pr[src]) | ((pr[nl] == pr[src]) & (nl > src))  # (priority, id) order
     blocked = np.zeros(V, bool)
     blocked[src[larger & inset[nl]]] = True  # has a larger neighbour in the set
     ok_mis = bool(np.all(np.isin(ms, [1, 2]))) and bool(np.all(inset == ~blocked))

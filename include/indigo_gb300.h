@@ -217,9 +217,10 @@ typedef struct ig_graph ig_graph;
 
 typedef struct ig_run_info {
   int status;         /* ig_status of the last run on this graph */
-  int iterations;     /* BFS levels, SSSP phases, MIS rounds, PR iterations */
-  long long work;     /* algorithm-specific counter (edges relaxed, wedges...) */
+  int iterations;     /* BFS levels, SSSP near iterations, MIS rounds, PR iterations */
+  long long work;     /* SSSP: distance improvements */
   double residual;    /* PR: last L1 residual */
+  long long aux[4];   /* SSSP: far-pile splits, frontier vertices, edges expanded, - */
 } ig_run_info;
 
 /* Binds caller-owned device CSR arrays (not copied, not freed). */

@@ -211,8 +211,29 @@ __global__ void __launch_bounds__(kThreads) pr_persistent(PrArgs a) {
       float sum = 0.f;
       const bool light = vi < a.nodes && d <= kLight;
       if (light) {
+        // loads issued four at a time so each lane keeps several gathers in
+        // flight; the adds stay in adjacency order
         float s = 0.f, c = 0.f;
-        for (int k = b; k < e; k++) kahan_add(s, c, cur[__ldg(&a.nlist[k])]);
+        int k = b;
+        for (; k + 4 <= e; k += 4) {
+          const int n0 = __ldg(&a.nlist[k]), n1 = __ldg(&a.nlist[k + 1]);
+          const int n2 = __ldg(&a.nlist[k + 2]), n3 = __ldg(&a.nlist[k + 3]);
+          const float x0 = cur[n0], x1 = cur[n1], x2 = cur[n2], x3 = cur[n3];
+          kahan_add(s, c, x0);
+          kahan_add(s, c, x1);
+          kahan_add(s, c, x2);
+          kahan_add(s, c, x3);
+        }
+        if (k < e) {
+          const int r = e - k;  // 1..3 left
+          const int n0 = __ldg(&a.nlist[k]);
+          const int n1 = r > 1 ? __ldg(&a.nlist[k + 1]) : n0;
+          const int n2 = r > 2 ? __ldg(&a.nlist[k + 2]) : n0;
+          const float x0 = cur[n0], x1 = cur[n1], x2 = cur[n2];
+          kahan_add(s, c, x0);
+          if (r > 1) kahan_add(s, c, x1);
+          if (r > 2) kahan_add(s, c, x2);
+        }
         sum = __fsub_rn(s, c);
       }
       unsigned med = __ballot_sync(IG_FULL, vi < a.nodes && d > kLight && d <= a.hub_degree);

@@ -583,6 +583,7 @@ extern "C" int ig_graph_last_run(ig_graph* g, ig_run_info* info) {
   info->iterations = g->h_ctl->iterations;
   info->work = g->h_ctl->work;
   info->residual = g->h_ctl->residual;
+  for (int i = 0; i < 4; i++) info->aux[i] = (long long)g->h_ctl->u64[12 + i];
   return IG_OK;
 }
 
@@ -636,7 +637,7 @@ IgOptions& ig_options() {
       /*blocks_per_sm=*/4,
       /*bfs_alpha=*/14,
       /*bfs_beta=*/24,
-      /*hub_degree=*/2048,
+      /*hub_degree=*/256,
       /*sssp_delta=*/0,
       /*sssp_delta_scale=*/32,
       /*pr_hub_degree=*/4096,

@@ -95,7 +95,7 @@ __global__ void __launch_bounds__(kThreads) sssp_persistent(SsspArgs a) {
   long long T = delta;  // distances < T are near
   int it = 0;           // near iteration index (stamp it+1 marks the next queue)
   int epoch = 0;
-  long long improved = 0;
+  long long improved = 0, frontier_v = 0, frontier_e = 0;
 
   while (true) {
     // ------------------------------------------------------------ near phase
@@ -142,6 +142,10 @@ __global__ void __launch_bounds__(kThreads) sssp_persistent(SsspArgs a) {
         }
         const bool hub = deg > a.hub_degree;
         warp_append(hub, u, a.hubs, nhub, a.nodes, ctl);
+        if (i < cur_size) {
+          frontier_v++;
+          frontier_e += deg;
+        }
         warp_expand(beg, hub ? 0 : deg, [&](bool act, int e, int j) {
           const int duj = __shfl_sync(IG_FULL, du, j);
           relax(act, e, duj);
@@ -214,9 +218,11 @@ __global__ void __launch_bounds__(kThreads) sssp_persistent(SsspArgs a) {
     if (done) break;
   }
   if (improved) atomicAdd((unsigned long long*)&ctl->work, (unsigned long long)improved);
+  if (frontier_v) atomicAdd(&ctl->u64[13], (unsigned long long)frontier_v);
+  if (frontier_e) atomicAdd(&ctl->u64[14], (unsigned long long)frontier_e);
   if (gtid == 0) {
     ctl->iterations = it;
-    ctl->i32[20] = epoch;
+    ctl->u64[12] = (unsigned long long)epoch;
   }
 }
 

@@ -50,6 +50,7 @@ class RunInfo(ctypes.Structure):
         ("iterations", ctypes.c_int),
         ("work", ctypes.c_longlong),
         ("residual", ctypes.c_double),
+        ("aux", ctypes.c_longlong * 4),
     ]
 
 

@@ -67,6 +67,7 @@ def main():
             mult = max(1, info.iterations) if args.algo == "pr" else 1
             gbs = bytes_per[args.algo] * mult / (ms * 1e-3) / 1e9
             print(f"{args.algo} run {r}: {ms:.3f} ms, iterations {info.iterations}, work {info.work}, "
+                  f"aux {list(info.aux)}, "
                   f"{E / (ms * 1e-3) / 1e9:.2f} GTEPS, {gbs:.0f} GB/s algorithmic (V={V}, E={E})")
         G.close()
 
