@@ -492,6 +492,107 @@ def run_reference(args, dist: Dist):
             "e2e": {"value": round(value, 4), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
 
 
+# ----------------------------------------------------------------------------- batched form
+BATCH_GRAPHS, BATCH_VMIN, BATCH_VMAX, BATCH_SEED = 4096, 1024, 65536, 13
+
+
+def run_batched(args, dist: Dist):
+    """Configuration 4: 4096 graphs (vertex counts log-uniform in [1k, 64k],
+    even Erdos-Renyi with average degree 8, odd RMAT with edge factor 8,
+    weights in [1, 255], seed 13).  One step = CC, BFS from vertex 0, TC and
+    PageRank of every graph with one batched call each (CUDA-graph replay);
+    value = graphs/s.  The plain comparison runs the same four algorithms as
+    one drop-in call per graph and algorithm (a sample of the graphs, scaled)."""
+    import indigo_gb300 as ig
+
+    ig.check(ig.load().ig_set_device(dist.local))
+    t0 = time.time()
+    u, vptr = ig.gen_batch(BATCH_GRAPHS, BATCH_VMIN, BATCH_VMAX, 8.0, 8, 0.57, 0.19, 0.19, BATCH_SEED, 255)
+    log(f"[bench] batch: {BATCH_GRAPHS} graphs, V={u.nodes} E={u.edges}, generated in {time.time() - t0:.1f}s")
+    b = ig.Batch(u, vptr)
+    V = u.nodes
+    d_dist, d_lab = ig.DeviceBuffer(4 * V), ig.DeviceBuffer(4 * V)
+    d_cnt, d_its = ig.DeviceBuffer(8 * b.graphs), ig.DeviceBuffer(4 * b.graphs)
+    sizes = np.diff(vptr)
+    init = np.repeat((np.float32(1.0) / sizes.astype(np.float32)).astype(np.float32), sizes)
+    d_init = ig.DeviceBuffer.from_array(init)
+    d_sc = ig.DeviceBuffer(4 * V)
+    L = ig.load()
+    ev = {k: (ig.Event(), ig.Event()) for k in ("bfs", "cc", "tc", "pr")}
+    acc = {k: 0.0 for k in ev}
+
+    def step(timed):
+        ev["cc"][0].record(b.stream)
+        b.cc(d_lab)
+        ev["cc"][1].record(b.stream)
+        ev["bfs"][0].record(b.stream)
+        b.bfs(d_dist)
+        ev["bfs"][1].record(b.stream)
+        ev["tc"][0].record(b.stream)
+        b.tc(d_cnt)
+        ev["tc"][1].record(b.stream)
+        ev["pr"][0].record(b.stream)
+        ig.check(L.ig_memcpy_async(d_sc.ptr, d_init.ptr, 4 * V, 3, b.stream))
+        b.pagerank(d_sc, PR_EPS, PR_MAX_ITER, d_its)
+        ev["pr"][1].record(b.stream)
+        if timed:
+            for k in ev:
+                acc[k] += ev[k][0].elapsed_ms(ev[k][1])
+
+    for _ in range(args.warmup):
+        step(False)
+    if b.last_run().status:
+        raise RuntimeError("batched run failed")
+    t_a, t_b = ig.Event(), ig.Event()
+    launches0 = ig.kernel_launches()
+    clocks = ClockSampler(dist.local)
+    dist.barrier()
+    b.synchronize()
+    t_a.record(b.stream)
+    for _ in range(args.steps):
+        step(True)
+    t_b.record(b.stream)
+    b.synchronize()
+    dist.barrier()
+    clk = clocks.stop()
+    launches = ig.kernel_launches() - launches0
+    if b.last_run().status:
+        raise RuntimeError("batched run failed during timing")
+    ms = dist.max(t_a.elapsed_ms(t_b)) / args.steps
+    value = dist.world * BATCH_GRAPHS / (ms * 1e-3)
+
+    # plain drop-in calls, one per graph and algorithm, on a sample of graphs
+    rng = np.random.default_rng(BATCH_SEED)
+    sample = np.sort(rng.choice(BATCH_GRAPHS, size=min(args.plain_sample, BATCH_GRAPHS), replace=False))
+    plain_s = 0.0
+    for i in sample:
+        g = ig.unpack(u, vptr, int(i))
+        with ig.DeviceCSR(g) as dg:
+            out = np.empty(g.nodes, np.int32)
+            sc = np.full(g.nodes, np.float32(1.0) / np.float32(g.nodes), np.float32)
+            deg = g.degree()
+            ig.check(L.ig_device_synchronize())
+            t1 = time.perf_counter()
+            ig.GPUcc_vertex(dg, out)
+            ig.GPUbfs_vertex(0, dg, out)
+            ig.GPUtc_vertex(g.nodes, dg.nindex_ptr, dg.nlist_ptr)
+            ig.PR_GPU(g, sc, deg, PR_EPS, PR_MAX_ITER)
+            plain_s += time.perf_counter() - t1
+    plain_value = len(sample) / plain_s
+    b.close()
+    return {"metric": "graphs/s (4096 packed graphs: CC + BFS + TC + PR per graph)", "value": round(value, 1),
+            "unit": "graphs/s", "n_gpus": dist.world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": round(ms, 3), "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "int32/f32", "data": "synthetic",
+            "config": {"workload": "batch4096_er8_rmat8", "graphs": BATCH_GRAPHS, "vertices": V, "edges": u.edges,
+                       "vmin": BATCH_VMIN, "vmax": BATCH_VMAX, "seed": BATCH_SEED,
+                       "l2": "inputs larger than L2 (%.0f MB neighbour lists)" % (4 * u.edges / 1e6)},
+            "per_algo_ms": {k: round(v / args.steps, 3) for k, v in acc.items()},
+            "plain": {"value": round(plain_value, 1), "unit": "graphs/s", "sample_graphs": int(len(sample)),
+                      "api": "drop-in C ABI, one call per graph and algorithm (host wall clock, results to host)"},
+            "speedup_vs_plain": round(value / plain_value, 1), "clocks": clk, "gpu_launches": launches}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -500,6 +601,9 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--form", choices=["plain", "batched"], default="plain",
+                    help="plain: the six algorithms on RMAT-22 (default); batched: 4096 packed graphs")
+    ap.add_argument("--plain-sample", type=int, default=256, help="graphs timed with plain calls (batched form)")
     args = ap.parse_args()
     if args.warmup < 3:
         log("[bench] warm-up raised to 3 (minimum)")
@@ -510,6 +614,8 @@ def main():
             if dist.rank != 0:
                 return
             out = run_reference(args, dist)
+        elif args.form == "batched":
+            out = run_batched(args, dist)
         else:
             out = run_ours(args, dist)
         if dist.rank == 0:

@@ -243,6 +243,40 @@ int ig_pagerank(ig_graph* g, float* d_scores, float epsilon, int max_iter);
 int ig_tc(ig_graph* g, unsigned long long* d_count);
 
 /* ---------------------------------------------------------------------------
+ * Batched form: many graphs packed as one disjoint union (no counterpart in
+ * the reference, which runs one program per graph).  d_union: device CSR of
+ * the union with global vertex ids; d_graph_vptr: device int[graphs+1], the
+ * first global vertex of each graph (d_graph_vptr[graphs] = d_union->nodes).
+ * Each algorithm is one launch sequence, captured into a CUDA graph on its
+ * second call and replayed afterwards; calls are asynchronous on the batch's
+ * stream.  Results equal the per-graph drop-in calls.
+ * ------------------------------------------------------------------------ */
+typedef struct ig_batch ig_batch;
+int ig_batch_create(const ig_csr* d_union, const int* d_graph_vptr, int graphs, ig_batch** out);
+int ig_batch_destroy(ig_batch* b);
+int ig_batch_stream(ig_batch* b, void** stream);
+/* 0: plain launches instead of CUDA-graph replay (for comparison). */
+int ig_batch_use_graphs(ig_batch* b, int enable);
+int ig_batch_last_run(ig_batch* b, ig_run_info* info);
+/* BFS levels of every graph from d_sources[g] (global ids; NULL: local
+ * vertex 0 of each graph); d_dist[v] indexed by global vertex. */
+int ig_batch_bfs(ig_batch* b, const int* d_sources, int* d_dist);
+/* Per-graph min-id component labels, as LOCAL ids, indexed by global vertex. */
+int ig_batch_cc(ig_batch* b, int* d_label);
+/* Triangles per graph: d_counts[g] (device unsigned long long[graphs]). */
+int ig_batch_tc(ig_batch* b, unsigned long long* d_counts);
+/* PageRank of every graph with its own (1-d)/V_g and its own stop rule;
+ * d_scores in/out by global vertex; d_iters[g] receives the iterations. */
+int ig_batch_pagerank(ig_batch* b, float* d_scores, float epsilon, int max_iter, int* d_iters);
+/* Host generator of a batch: `graphs` graphs with vertex counts log-uniform
+ * in [vmin, vmax]; even indices Erdos-Renyi (average degree er_degree), odd
+ * ones RMAT (a, b, c; rmat_edge_factor pairs per vertex, ids taken modulo the
+ * vertex count), each symmetric, sorted, simple, weights in [1, maxw];
+ * returned packed as a union CSR (malloc'ed) and out_vptr[graphs+1]. */
+int ig_gen_batch(int graphs, int vmin, int vmax, double er_degree, int rmat_edge_factor, double a, double b,
+                 double c, uint64_t seed, int maxw, ig_csr* out_union, int* out_vptr);
+
+/* ---------------------------------------------------------------------------
  * Self-test (no counterpart in the reference, whose waits are host-side)
  * ------------------------------------------------------------------------ */
 /* Launches a persistent kernel in which one block never reaches the grid

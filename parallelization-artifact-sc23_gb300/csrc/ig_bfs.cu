@@ -41,6 +41,8 @@ struct BfsArgs {
   int hub_degree;
   int alpha;
   int beta;
+  const int* sources;  // batched form: one source per graph of a disjoint union (else null)
+  int nsources;
 };
 
 // ctl->i32[s] : size of the queue built during a level with slot s (= level % 3)
@@ -55,15 +57,28 @@ __global__ void __launch_bounds__(kThreads) bfs_persistent(BfsArgs a) {
   const int warp_g = (int)(gtid >> 5);
   const int nwarps = (int)(gthreads >> 5);
 
-  for (long long v = gtid; v < a.nodes; v += gthreads) a.dist[v] = (v == a.src) ? 0 : kInf;
-  if (gtid == 0) a.qa[0] = a.src;
+  long long src_deg = 0;
+  int cur_size = 1;
+  if (a.sources == nullptr) {
+    for (long long v = gtid; v < a.nodes; v += gthreads) a.dist[v] = (v == a.src) ? 0 : kInf;
+    if (gtid == 0) a.qa[0] = a.src;
+    src_deg = __ldg(&a.nindex[a.src + 1]) - __ldg(&a.nindex[a.src]);
+  } else {
+    // several sources (one per graph of a disjoint union): all start at level 0
+    for (long long v = gtid; v < a.nodes; v += gthreads) a.dist[v] = kInf;
+    if (!grid_sync(ctl, a.timeout_ns)) return;
+    for (long long i = gtid; i < a.nsources; i += gthreads) {
+      a.dist[a.sources[i]] = 0;
+      a.qa[i] = a.sources[i];
+    }
+    cur_size = a.nsources;
+    src_deg = a.edges / 2;  // start top-down; the switch rule takes over after level 0
+  }
   if (!grid_sync(ctl, a.timeout_ns)) return;
 
   int* cur = a.qa;
   int* nxt = a.qb;
-  int cur_size = 1;
   bool bottom_up = false;
-  const long long src_deg = __ldg(&a.nindex[a.src + 1]) - __ldg(&a.nindex[a.src]);
   long long unexplored = a.edges - src_deg;
   int level = 0;
 
@@ -162,7 +177,24 @@ int igk_bfs(IgExec* ex, const ig_csr* dg, int src, int* d_dist) {
   if ((rc = ig_exec_reset(ex))) return rc;
   const IgOptions& o = ig_options();
   BfsArgs a{dg->nindex, dg->nlist, dg->nodes, dg->edges, src, d_dist, (int*)qa, (int*)qb, (int*)hubs,
-            ex->d_ctl, ex->timeout_ns, o.hub_degree, o.bfs_alpha, o.bfs_beta};
+            ex->d_ctl, ex->timeout_ns, o.hub_degree, o.bfs_alpha, o.bfs_beta, nullptr, 0};
+  void* args[] = {&a};
+  return ig_launch_coop(ex, (const void*)bfs_persistent, kThreads, 0, o.blocks_per_sm, args, nullptr);
+}
+
+// Multi-source form for a disjoint union of graphs: d_sources[i] (global ids,
+// one per graph) all start at level 0, so each graph gets its own BFS levels.
+int igk_bfs_multi(IgExec* ex, const ig_csr* dg, const int* d_sources, int nsources, int* d_dist) {
+  const size_t vb = (size_t)dg->nodes * sizeof(int);
+  void *qa, *qb, *hubs;
+  int rc;
+  if ((rc = ig_scratch_get(ex->scratch, IG_SLOT_Q0, vb, &qa))) return rc;
+  if ((rc = ig_scratch_get(ex->scratch, IG_SLOT_Q1, vb, &qb))) return rc;
+  if ((rc = ig_scratch_get(ex->scratch, IG_SLOT_Q2, vb, &hubs))) return rc;
+  if ((rc = ig_exec_reset(ex))) return rc;
+  const IgOptions& o = ig_options();
+  BfsArgs a{dg->nindex, dg->nlist, dg->nodes, dg->edges, 0, d_dist, (int*)qa, (int*)qb, (int*)hubs,
+            ex->d_ctl, ex->timeout_ns, o.hub_degree, o.bfs_alpha, o.bfs_beta, d_sources, nsources};
   void* args[] = {&a};
   return ig_launch_coop(ex, (const void*)bfs_persistent, kThreads, 0, o.blocks_per_sm, args, nullptr);
 }
@@ -180,7 +212,7 @@ int igk_bfs_launch_prealloc(IgExec* ex, const ig_csr* dg, int src, int* d_dist, 
   if (o.blocks_per_sm > 0) per_sm = std::min(per_sm, o.blocks_per_sm);
   if (per_sm < 1) return ig_fail(IG_ERR_CUDA, "persistent kernel cannot be resident (occupancy 0)");
   BfsArgs a{dg->nindex, dg->nlist, dg->nodes, dg->edges, src, d_dist, qa, qb, hubs,
-            ex->d_ctl, ex->timeout_ns, o.hub_degree, o.bfs_alpha, o.bfs_beta};
+            ex->d_ctl, ex->timeout_ns, o.hub_degree, o.bfs_alpha, o.bfs_beta, nullptr, 0};
   void* args[] = {&a};
   rc = ig_cuda_check((int)cudaLaunchCooperativeKernel((const void*)bfs_persistent, dim3(per_sm * ex->sms),
                                                       dim3(kThreads), args, 0, ex->stream),

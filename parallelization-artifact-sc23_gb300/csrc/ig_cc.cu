@@ -121,7 +121,22 @@ __global__ void cc_compress(int* parent, int n) {
   }
 }
 
+// Disjoint union of graphs: the global min-id label minus the graph's first
+// vertex is the graph's own min-id label.  One block per graph.
+__global__ void cc_localize(int* label, const int* __restrict__ graph_vptr, int graphs) {
+  for (int g = blockIdx.x; g < graphs; g += gridDim.x) {
+    const int b = __ldg(&graph_vptr[g]), e = __ldg(&graph_vptr[g + 1]);
+    for (int v = b + threadIdx.x; v < e; v += blockDim.x) label[v] -= b;
+  }
+}
+
 }  // namespace
+
+int igk_cc_localize(IgExec* ex, int* d_label, const int* d_graph_vptr, int graphs) {
+  cc_localize<<<std::min(graphs, ex->sms * 16), kThreads, 0, ex->stream>>>(d_label, d_graph_vptr, graphs);
+  ig_count_launches(1);
+  return ig_cuda_check((int)cudaGetLastError(), "cc localize launch");
+}
 
 int igk_cc(IgExec* ex, const ig_csr* dg, int* d_label) {
   const int n = dg->nodes;

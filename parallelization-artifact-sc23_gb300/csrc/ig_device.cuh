@@ -345,3 +345,124 @@ __device__ __forceinline__ double block_sum_double(double x, double* tmp) {
 }
 
 }  // namespace ig
+
+namespace ig {
+
+// Warp-aggregated append of up to kMax items per lane (items[0..cnt)): one
+// atomicAdd per warp.  All lanes of a converged warp call it.
+template <int kMax>
+__device__ __forceinline__ void warp_append_n(int cnt, const int (&items)[kMax], int* q, int* qsize, int cap,
+                                              IgCtl* ctl) {
+  const int lane = lane_id();
+  int incl = cnt;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int t = __shfl_up_sync(IG_FULL, incl, o);
+    if (lane >= o) incl += t;
+  }
+  const int total = __shfl_sync(IG_FULL, incl, 31);
+  if (total == 0) return;
+  int base = 0;
+  if (lane == 31) base = atomicAdd(qsize, total);
+  base = __shfl_sync(IG_FULL, base, 31) + incl - cnt;
+#pragma unroll
+  for (int k = 0; k < kMax; k++) {
+    if (k < cnt) {
+      if (base + k < cap) q[base + k] = items[k];
+      else raise(ctl, IG_ERR_OVERFLOW);
+    }
+  }
+}
+
+// Load-balanced expansion like warp_expand, four 32-edge steps at a time:
+// visit4(act[4], edge[4], owner_lane[4]) is called warp-uniformly with the
+// four slots of each lane, so the callee can issue their memory operations
+// together (more loads in flight per lane than one step at a time).
+template <class Visit4>
+__device__ __forceinline__ void warp_expand4(int beg, int deg, Visit4&& visit4) {
+  const int lane = lane_id();
+  int incl = deg;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int t = __shfl_up_sync(IG_FULL, incl, o);
+    if (lane >= o) incl += t;
+  }
+  const int total = __shfl_sync(IG_FULL, incl, 31);
+  const int excl = incl - deg;
+  for (int base = 0; base < total; base += 128) {
+    bool act[4];
+    int edge[4], own[4];
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+      const int e = base + k * 32 + lane;
+      int j = 0;
+#pragma unroll
+      for (int step = 16; step >= 1; step >>= 1) {
+        const int ex = __shfl_sync(IG_FULL, excl, j + step);
+        if (ex <= e) j += step;
+      }
+      const int jb = __shfl_sync(IG_FULL, beg, j);
+      const int je = __shfl_sync(IG_FULL, excl, j);
+      act[k] = e < total;
+      edge[k] = jb + (e - je);
+      own[k] = j;
+    }
+    visit4(act, edge, own);
+  }
+}
+
+}  // namespace ig
+
+namespace ig {
+
+// grid_expand_hubs with four grid-strided edge slots per thread per round:
+// visit4(act[4], edge[4], hub_vertex[4]) is called warp-uniformly.
+template <class Visit4>
+__device__ __forceinline__ void grid_expand_hubs4(const int* __restrict__ nindex, const int* hubs, int nh,
+                                                  Visit4&& visit4) {
+  __shared__ long long s_pref[kHubBatch + 1];
+  __shared__ int s_beg[kHubBatch];
+  __shared__ int s_v[kHubBatch];
+  __shared__ long long s_warp[32];
+  const long long gthreads = (long long)gridDim.x * blockDim.x;
+  for (int hb = 0; hb < nh; hb += kHubBatch) {
+    const int cnt = min(kHubBatch, nh - hb);
+    __syncthreads();
+    for (int i = threadIdx.x; i < cnt; i += blockDim.x) {
+      const int v = hubs[hb + i];
+      const int b = __ldg(&nindex[v]);
+      s_v[i] = v;
+      s_beg[i] = b;
+      s_pref[i] = __ldg(&nindex[v + 1]) - b;
+    }
+    __syncthreads();
+    block_exclusive_scan64(s_pref, cnt, s_warp);
+    const long long total = s_pref[cnt];
+    const long long wbase = (long long)blockIdx.x * blockDim.x + (threadIdx.x & ~31);
+    for (long long base = wbase; base < total; base += 4 * gthreads) {
+      bool act[4];
+      int edge[4], hv[4];
+#pragma unroll
+      for (int k = 0; k < 4; k++) {
+        const long long e = base + k * gthreads + lane_id();
+        act[k] = e < total;
+        int h = 0;
+        if (act[k]) {
+          int lo = 0, hi = cnt - 1;
+          while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (s_pref[mid] <= e) lo = mid;
+            else hi = mid - 1;
+          }
+          h = lo;
+        }
+        edge[k] = act[k] ? s_beg[h] + (int)(e - s_pref[h]) : 0;
+        hv[k] = act[k] ? s_v[h] : 0;
+      }
+      visit4(act, edge, hv);
+    }
+  }
+  __syncthreads();
+}
+
+}  // namespace ig

@@ -168,10 +168,14 @@ static int hw_threads() {
   return (int)std::min(n, 64u);
 }
 
+// Set inside per-graph workers of ig_gen_batch, which run many small graphs
+// in parallel: their inner loops then stay on the calling thread.
+static thread_local bool t_serial = false;
+
 template <class F>
 static void parallel_for(long long n, F&& f) {
   const int T = hw_threads();
-  if (n < 65536 || T == 1) {
+  if (n < 65536 || T == 1 || t_serial) {
     f(0LL, n, 0);
     return;
   }
@@ -478,4 +482,107 @@ extern "C" uint64_t ig_csr_digest(const ig_csr* g) {
   if (g->nlist) h = fnv(h, g->nlist, (size_t)g->edges * sizeof(int));
   if (g->eweight) h = fnv(h, g->eweight, (size_t)g->edges * sizeof(int));
   return h;
+}
+
+// RMAT pairs on n vertices (ids drawn at the next power of two, taken mod n).
+static void rmat_pairs(int n, long long m, double a, double b, double c, const Rng& r, std::vector<int>& us,
+                       std::vector<int>& vs) {
+  int scale = 0;
+  while ((1LL << scale) < n) scale++;
+  const uint32_t ta = (uint32_t)std::min(4294967295.0, a * 4294967296.0);
+  const uint32_t tb = (uint32_t)std::min(4294967295.0, (a + b) * 4294967296.0);
+  const uint32_t tc = (uint32_t)std::min(4294967295.0, (a + b + c) * 4294967296.0);
+  us.resize((size_t)m);
+  vs.resize((size_t)m);
+  for (long long k = 0; k < m; k++) {
+    long long u = 0, v = 0;
+    uint64_t bits = 0;
+    for (int lev = 0; lev < scale; lev++) {
+      if ((lev & 1) == 0) bits = r.at((uint64_t)k * 16 + (uint64_t)(lev >> 1));
+      const uint32_t x = (uint32_t)(bits >> ((lev & 1) * 32));
+      u = (u << 1) | ((x >= tb) ? 1 : 0);
+      v = (v << 1) | (((x >= ta && x < tb) || x >= tc) ? 1 : 0);
+    }
+    us[k] = (int)(u % n);
+    vs[k] = (int)(v % n);
+  }
+}
+
+extern "C" int ig_gen_batch(int graphs, int vmin, int vmax, double er_degree, int rmat_edge_factor, double a,
+                            double b, double c, uint64_t seed, int maxw, ig_csr* out_union, int* out_vptr) {
+  if (graphs < 1 || vmin < 2 || vmax < vmin || !out_union || !out_vptr || er_degree < 0 || rmat_edge_factor < 0)
+    return ig_fail(IG_ERR_INVALID_ARG, "ig_gen_batch: bad parameters");
+  std::vector<ig_csr> parts((size_t)graphs);
+  std::vector<int> rcs((size_t)graphs, IG_OK);
+  const Rng sizes(seed, 0xb47c);
+  std::atomic<int> next{0};
+  const int T = hw_threads();
+  std::vector<std::thread> th;
+  for (int t = 0; t < T; t++) {
+    th.emplace_back([&] {
+      t_serial = true;
+      for (int i = next.fetch_add(1); i < graphs; i = next.fetch_add(1)) {
+        const double lo = std::log((double)vmin), hi = std::log((double)vmax);
+        const int n = std::max(vmin, std::min(vmax, (int)llround(std::exp(lo + (hi - lo) * sizes.uniform((uint64_t)i)))));
+        const uint64_t gseed = seed * 0x9E3779B97F4A7C15ull + (uint64_t)i;
+        std::vector<int> us, vs;
+        if ((i & 1) == 0) {
+          const long long m = (long long)llround((double)n * er_degree / 2.0);
+          const Rng r(gseed, 0xe7);
+          us.resize((size_t)m);
+          vs.resize((size_t)m);
+          for (long long k = 0; k < m; k++) {
+            us[k] = (int)(r.at((uint64_t)(2 * k)) % (uint64_t)n);
+            vs[k] = (int)(r.at((uint64_t)(2 * k + 1)) % (uint64_t)n);
+          }
+        } else {
+          const Rng r(gseed, 0x5a7);
+          rmat_pairs(n, (long long)n * rmat_edge_factor, a, b, c, r, us, vs);
+        }
+        rcs[i] = build_csr(n, us, vs, maxw, gseed, &parts[i]);
+      }
+    });
+  }
+  for (auto& x : th) x.join();
+  for (int i = 0; i < graphs; i++)
+    if (rcs[i] != IG_OK) {
+      for (auto& p : parts) ig_csr_free_host(&p);
+      return rcs[i];
+    }
+  long long V = 0, E = 0;
+  for (int i = 0; i < graphs; i++) {
+    out_vptr[i] = (int)V;
+    V += parts[i].nodes;
+    E += parts[i].edges;
+  }
+  out_vptr[graphs] = (int)V;
+  if (V > INT32_MAX || E > INT32_MAX) {
+    for (auto& p : parts) ig_csr_free_host(&p);
+    return ig_fail(IG_ERR_OVERFLOW, "batch exceeds 2^31-1 vertices or edges");
+  }
+  ig_csr u{(int)V, (int)E, nullptr, nullptr, nullptr};
+  u.nindex = (int*)malloc(((size_t)V + 1) * sizeof(int));
+  u.nlist = (int*)malloc(std::max<size_t>(1, (size_t)E) * sizeof(int));
+  if (maxw > 0) u.eweight = (int*)malloc(std::max<size_t>(1, (size_t)E) * sizeof(int));
+  if (!u.nindex || !u.nlist || (maxw > 0 && !u.eweight)) {
+    ig_csr_free_host(&u);
+    for (auto& p : parts) ig_csr_free_host(&p);
+    return ig_fail(IG_ERR_NOMEM, "allocation failed");
+  }
+  std::vector<long long> eoff((size_t)graphs + 1, 0);
+  for (int i = 0; i < graphs; i++) eoff[i + 1] = eoff[i] + parts[i].edges;
+  parallel_for(graphs, [&](long long lo, long long hi, int) {
+    for (long long i = lo; i < hi; i++) {
+      const ig_csr& p = parts[i];
+      const int vo = out_vptr[i];
+      const long long eo = eoff[i];
+      for (int v = 0; v < p.nodes; v++) u.nindex[vo + v] = (int)(eo + p.nindex[v]);
+      for (int e = 0; e < p.edges; e++) u.nlist[eo + e] = p.nlist[e] + vo;
+      if (maxw > 0) memcpy(u.eweight + eo, p.eweight, (size_t)p.edges * sizeof(int));
+    }
+  });
+  u.nindex[V] = (int)E;
+  for (auto& p : parts) ig_csr_free_host(&p);
+  *out_union = u;
+  return IG_OK;
 }

@@ -128,5 +128,12 @@ int igk_pr(IgExec* ex, const ig_csr* dg, const int* d_degree, float* d_scores,
            float epsilon, int max_iter);
 int igk_tc(IgExec* ex, int nodes, int edges, const int* d_nindex, const int* d_nlist,
            unsigned long long* d_count);
+// Batched (disjoint union) forms
+int igk_bfs_multi(IgExec* ex, const ig_csr* dg, const int* d_sources, int nsources, int* d_dist);
+int igk_cc_localize(IgExec* ex, int* d_label, const int* d_graph_vptr, int graphs);
+int igk_tc_batched(IgExec* ex, int nodes, int edges, const int* d_nindex, const int* d_nlist,
+                   const int* d_graph_vptr, int graphs, unsigned long long* d_counts);
+int igk_pr_batched(IgExec* ex, const ig_csr* dg, const int* d_graph_vptr, int graphs, float* d_scores,
+                   float epsilon, int max_iter, int* d_iters);
 // Device-wide exclusive scan of n ints (n+1 outputs, out[n] = total) into out.
 int igk_exclusive_scan(IgExec* ex, const int* in, int* out, int n, long long* total_host);

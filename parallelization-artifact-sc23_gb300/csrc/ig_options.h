@@ -8,6 +8,7 @@ struct IgOptions {
   int hub_degree;         // degree above which a vertex is expanded by the whole grid
   long long sssp_delta;   // near/far bucket width (0 = derived from sampled weights)
   int sssp_delta_scale;   // derived width = mean weight * scale / mean degree
+  int sssp_heavy_split;   // 1: heavy edges (w >= delta) relaxed once per bucket
   int pr_hub_degree;      // PageRank: degree above which a vertex is split in chunks
   int pr_chunk;           // PageRank: edges per hub chunk
 };

@@ -52,7 +52,39 @@ struct PrArgs {
   unsigned long long timeout_ns;
   int hub_degree;
   int chunk;
+  // batched form (disjoint union of graphs): first vertex of each graph,
+  // per-graph residuals (3 rotating slots) and per-graph iteration counts
+  const int* graph_vptr;
+  int graphs;
+  double* gres;
+  int* giters;
 };
+
+// graph of vertex v: largest g with graph_vptr[g] <= v
+__device__ __forceinline__ int graph_of(const PrArgs& a, int v) {
+  int lo = 0, hi = a.graphs - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (__ldg(&a.graph_vptr[mid]) <= v) lo = mid;
+    else hi = mid - 1;
+  }
+  return lo;
+}
+
+// Adds each lane's x into gres[g_lane] with one atomic per distinct graph of the warp.
+__device__ __forceinline__ void warp_add_by_graph(double* gres, int g, double x, bool valid) {
+  unsigned rem = __ballot_sync(IG_FULL, valid);
+  while (rem) {
+    const int leader = __ffs(rem) - 1;
+    const int gl = __shfl_sync(IG_FULL, g, leader);
+    const bool in = valid && g == gl;
+    double v = in ? x : 0.0;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(IG_FULL, v, o);
+    if (ig::lane_id() == leader && v != 0.0) atomicAdd(&gres[gl], v);
+    rem &= ~__ballot_sync(IG_FULL, in);
+  }
+}
 
 __device__ __forceinline__ void kahan_add(float& s, float& c, float x) {
   const float y = __fsub_rn(x, c);
@@ -104,6 +136,7 @@ __device__ __forceinline__ int vdegree(const PrArgs& a, int v) {
   return a.degree ? a.degree[v] : (__ldg(&a.nindex[v + 1]) - __ldg(&a.nindex[v]));
 }
 
+template <bool kBatched>
 __global__ void __launch_bounds__(kThreads) pr_persistent(PrArgs a) {
   using namespace ig;
   __shared__ int s_scan[33];
@@ -183,6 +216,15 @@ __global__ void __launch_bounds__(kThreads) pr_persistent(PrArgs a) {
   while (it < a.max_iter) {
     it++;
     double err = 0;
+    // batched: a graph whose residual fell below epsilon stops changing (its
+    // scores are final after that iteration, as for a single-graph run)
+    double* gcur = kBatched ? a.gres + (it % 3) * a.graphs : nullptr;
+    const double* gprev = kBatched ? a.gres + ((it + 2) % 3) * a.graphs : nullptr;
+    if (kBatched) {
+      double* gnext = a.gres + ((it + 1) % 3) * a.graphs;
+      for (long long g = gtid; g < a.graphs; g += gthreads) gnext[g] = 0.0;
+    }
+    auto frozen = [&](int g) { return kBatched && it > 1 && ld_relaxed(&gprev[g]) < (double)a.eps; };
     // ---- phase A: hub chunks (partial sums) and regular vertices
     for (int c = warp_g; c < nchunks; c += nwarps) {
       // owning hub: largest h with chunk_base[h] <= c
@@ -193,6 +235,7 @@ __global__ void __launch_bounds__(kThreads) pr_persistent(PrArgs a) {
         else hi = mid - 1;
       }
       const int hv = a.hubs[lo];
+      if (kBatched && frozen(graph_of(a, hv))) continue;
       const int hb = __ldg(&a.nindex[hv]), he = __ldg(&a.nindex[hv + 1]);
       const int b = hb + (c - a.chunk_base[lo]) * a.chunk;
       const int e = min(b + a.chunk, he);
@@ -207,9 +250,19 @@ __global__ void __launch_bounds__(kThreads) pr_persistent(PrArgs a) {
         b = __ldg(&a.nindex[v]);
         e = __ldg(&a.nindex[v + 1]);
       }
-      const int d = e - b;
+      int d = e - b;
       float sum = 0.f;
-      const bool light = vi < a.nodes && d <= kLight;
+      int vg = 0;
+      float vbase = a.base;
+      bool skip = false;
+      if (kBatched && vi < a.nodes) {
+        vg = graph_of(a, v);
+        skip = frozen(vg);
+        vbase = __fdiv_rn(__fsub_rn(1.0f, a.damp),
+                          (float)(__ldg(&a.graph_vptr[vg + 1]) - __ldg(&a.graph_vptr[vg])));
+      }
+      if (skip) d = a.hub_degree + 1;  // handled by nobody: frozen
+      const bool light = vi < a.nodes && !skip && d <= kLight;
       if (light) {
         // loads issued four at a time so each lane keeps several gathers in
         // flight; the adds stay in adjacency order
@@ -236,7 +289,7 @@ __global__ void __launch_bounds__(kThreads) pr_persistent(PrArgs a) {
         }
         sum = __fsub_rn(s, c);
       }
-      unsigned med = __ballot_sync(IG_FULL, vi < a.nodes && d > kLight && d <= a.hub_degree);
+      unsigned med = __ballot_sync(IG_FULL, vi < a.nodes && !skip && d > kLight && d <= a.hub_degree);
       while (med) {
         const int l = __ffs(med) - 1;
         med &= med - 1;
@@ -245,13 +298,17 @@ __global__ void __launch_bounds__(kThreads) pr_persistent(PrArgs a) {
         warp_gather_sum(a.nlist, cur, mb, me, shi, slo);
         if (lane == l) sum = __fadd_rn(shi, slo);
       }
-      if (vi < a.nodes && d <= a.hub_degree) {
+      double verr = 0.0;
+      const bool upd = vi < a.nodes && !skip && d <= a.hub_degree;
+      if (upd) {
         const float old = a.scores[v];
-        const float nw = __fadd_rn(a.base, __fmul_rn(a.damp, sum));
+        const float nw = __fadd_rn(vbase, __fmul_rn(a.damp, sum));
         a.scores[v] = nw;
         nxt[v] = __fdiv_rn(nw, (float)vdegree(a, v));
-        err += (double)fabsf(__fsub_rn(nw, old));
+        verr = (double)fabsf(__fsub_rn(nw, old));
+        err += verr;
       }
+      if (kBatched) warp_add_by_graph(gcur, vg, verr, upd);
     }
     // ---- phase B: combine hub chunks in chunk order
     if (nh > 0) {
@@ -264,14 +321,24 @@ __global__ void __launch_bounds__(kThreads) pr_persistent(PrArgs a) {
           pair_add(hi, lo, p.x, p.y);
         }
         warp_pair_reduce(hi, lo);
+        const int v = a.hubs[h];
+        int hg = 0;
+        float hbase = a.base;
+        if (kBatched) {
+          hg = graph_of(a, v);
+          if (frozen(hg)) continue;
+          hbase = __fdiv_rn(__fsub_rn(1.0f, a.damp),
+                            (float)(__ldg(&a.graph_vptr[hg + 1]) - __ldg(&a.graph_vptr[hg])));
+        }
         if (lane == 0) {
-          const int v = a.hubs[h];
           const float sum = __fadd_rn(hi, lo);
           const float old = a.scores[v];
-          const float nw = __fadd_rn(a.base, __fmul_rn(a.damp, sum));
+          const float nw = __fadd_rn(hbase, __fmul_rn(a.damp, sum));
           a.scores[v] = nw;
           nxt[v] = __fdiv_rn(nw, (float)vdegree(a, v));
-          err += (double)fabsf(__fsub_rn(nw, old));
+          const double herr = (double)fabsf(__fsub_rn(nw, old));
+          err += herr;
+          if (kBatched && herr != 0.0) atomicAdd(&gcur[hg], herr);
         }
       }
     }
@@ -284,8 +351,27 @@ __global__ void __launch_bounds__(kThreads) pr_persistent(PrArgs a) {
     float* t = cur;
     cur = nxt;
     nxt = t;
-    if (residual < (double)a.eps) break;
+    if (!kBatched) {
+      if (residual < (double)a.eps) break;
+    } else {
+      // record each graph's iteration count when it converges; stop when all did
+      __shared__ int s_active;
+      if (threadIdx.x == 0) s_active = 0;
+      __syncthreads();
+      int active = 0;
+      for (int g = threadIdx.x; g < a.graphs; g += blockDim.x) {
+        const bool conv = ld_relaxed(&gcur[g]) < (double)a.eps;
+        if (!conv) active = 1;
+        if (blockIdx.x == 0 && conv && a.giters[g] == 0) a.giters[g] = it;
+      }
+      if (active) s_active = 1;
+      __syncthreads();
+      if (s_active == 0) break;
+    }
   }
+  if (kBatched && blockIdx.x == 0)
+    for (int g = threadIdx.x; g < a.graphs; g += blockDim.x)
+      if (a.giters[g] == 0) a.giters[g] = it;
   if (gtid == 0) {
     ctl->iterations = it;
     ctl->residual = residual;
@@ -294,7 +380,8 @@ __global__ void __launch_bounds__(kThreads) pr_persistent(PrArgs a) {
 
 }  // namespace
 
-int igk_pr(IgExec* ex, const ig_csr* dg, const int* d_degree, float* d_scores, float epsilon, int max_iter) {
+static int pr_launch(IgExec* ex, const ig_csr* dg, const int* d_degree, float* d_scores, float epsilon,
+                     int max_iter, const int* d_graph_vptr, int graphs, int* d_iters) {
   const IgOptions& o = ig_options();
   const int n = dg->nodes;
   const int hub_degree = std::max(o.pr_hub_degree, 32);
@@ -302,7 +389,7 @@ int igk_pr(IgExec* ex, const ig_csr* dg, const int* d_degree, float* d_scores, f
   const long long max_hubs = (long long)dg->edges / (hub_degree + 1) + 1;
   const long long max_chunks = (long long)dg->edges / chunk + max_hubs + 1;
   const int max_blocks = ex->sms * 32;
-  void *ca, *cb, *hubs, *cbase, *part, *blk, *blkerr;
+  void *ca, *cb, *hubs, *cbase, *part, *blk, *blkerr, *gres = nullptr;
   int rc;
   if ((rc = ig_scratch_get(ex->scratch, IG_SLOT_F0, (size_t)n * sizeof(float), &ca))) return rc;
   if ((rc = ig_scratch_get(ex->scratch, IG_SLOT_F1, (size_t)n * sizeof(float), &cb))) return rc;
@@ -311,13 +398,30 @@ int igk_pr(IgExec* ex, const ig_csr* dg, const int* d_degree, float* d_scores, f
   if ((rc = ig_scratch_get(ex->scratch, IG_SLOT_Q2, (size_t)max_chunks * sizeof(float2), &part))) return rc;
   if ((rc = ig_scratch_get(ex->scratch, IG_SLOT_V0, (size_t)2 * max_blocks * sizeof(int), &blk))) return rc;
   if ((rc = ig_scratch_get(ex->scratch, IG_SLOT_BLK, (size_t)2 * max_blocks * sizeof(double), &blkerr))) return rc;
+  if (d_graph_vptr) {
+    if ((rc = ig_scratch_get(ex->scratch, IG_SLOT_V1, (size_t)3 * graphs * sizeof(double), &gres))) return rc;
+    if ((rc = ig_cuda_check((int)cudaMemsetAsync(gres, 0, (size_t)3 * graphs * sizeof(double), ex->stream), "memset")))
+      return rc;
+    if ((rc = ig_cuda_check((int)cudaMemsetAsync(d_iters, 0, (size_t)graphs * sizeof(int), ex->stream), "memset")))
+      return rc;
+  }
   if ((rc = ig_exec_reset(ex))) return rc;
   const float damp = 0.85f;
   const float base = (1.0f - damp) / (float)n;
   PrArgs a{dg->nindex, dg->nlist, d_degree, n, dg->edges, d_scores, (float*)ca, (float*)cb, (int*)hubs,
            (int*)cbase, (float2*)part, (int*)blk, (double*)blkerr, ex->d_ctl, epsilon, max_iter, base, damp,
-           ex->timeout_ns, hub_degree, chunk};
+           ex->timeout_ns, hub_degree, chunk, d_graph_vptr, graphs, (double*)gres, d_iters};
   void* args[] = {&a};
-  int cap = o.blocks_per_sm > 0 ? std::min(o.blocks_per_sm, 32) : 32;
-  return ig_launch_coop(ex, (const void*)pr_persistent, kThreads, 0, cap, args, nullptr);
+  const int cap = o.blocks_per_sm > 0 ? std::min(o.blocks_per_sm, 32) : 32;
+  const void* fn = d_graph_vptr ? (const void*)pr_persistent<true> : (const void*)pr_persistent<false>;
+  return ig_launch_coop(ex, fn, kThreads, 0, cap, args, nullptr);
+}
+
+int igk_pr(IgExec* ex, const ig_csr* dg, const int* d_degree, float* d_scores, float epsilon, int max_iter) {
+  return pr_launch(ex, dg, d_degree, d_scores, epsilon, max_iter, nullptr, 0, nullptr);
+}
+
+int igk_pr_batched(IgExec* ex, const ig_csr* dg, const int* d_graph_vptr, int graphs, float* d_scores,
+                   float epsilon, int max_iter, int* d_iters) {
+  return pr_launch(ex, dg, nullptr, d_scores, epsilon, max_iter, d_graph_vptr, graphs, d_iters);
 }

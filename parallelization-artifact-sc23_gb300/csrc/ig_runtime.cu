@@ -639,7 +639,8 @@ IgOptions& ig_options() {
       /*bfs_beta=*/24,
       /*hub_degree=*/256,
       /*sssp_delta=*/0,
-      /*sssp_delta_scale=*/32,
+      /*sssp_delta_scale=*/128,
+      /*sssp_heavy_split=*/0,
       /*pr_hub_degree=*/4096,
       /*pr_chunk=*/4096,
   };
@@ -658,6 +659,7 @@ struct OptField {
 static const OptField g_opt_fields[] = {
     IG_OPT(blocks_per_sm, 0, 32),     IG_OPT(bfs_alpha, 1, 1000000),   IG_OPT(bfs_beta, 1, 1000000),
     IG_OPT(hub_degree, 32, INT_MAX),  IG_OPT(sssp_delta, 0, INT_MAX),  IG_OPT(sssp_delta_scale, 1, 1 << 20),
+    IG_OPT(sssp_heavy_split, 0, 1),
     IG_OPT(pr_hub_degree, 32, INT_MAX), IG_OPT(pr_chunk, 32, 1 << 24),
 };
 

@@ -13,7 +13,9 @@
 // Near phase: the near queue is expanded 32 vertices per warp (hubs by the
 // whole grid); an improved vertex with distance < T joins the next near queue
 // (once per iteration, by stamp) and otherwise the far pile (once per epoch,
-// by flag).  When the near queue runs dry the far pile is split: the minimum
+// by flag).  A queued vertex is expanded only if its distance is below the
+// one it was last expanded with (re-queued vertices are often expanded
+// already).  When the near queue runs dry the far pile is split: the minimum
 // pending distance m is found, T becomes max(T, m) + delta, entries below the
 // old T are stale (already settled through the near queue) and dropped,
 // entries below the new T form the next near queue, the rest stay far.
@@ -40,11 +42,15 @@ struct SsspArgs {
   int* stamp;    // near-queue membership stamp
   int* farflag;  // far-pile membership (epoch + 1)
   int* hubs;
+  int* expanded;  // distance each vertex was last expanded with (INT_MAX: never)
+  int* members;   // vertices light-expanded since the last heavy pass
+  int* inmember;  // 1 while a vertex sits in members
   IgCtl* ctl;
   unsigned long long timeout_ns;
   int hub_degree;
   long long delta;       // > 0: fixed bucket width
   int delta_scale;
+  int heavy_split;       // 1: light/heavy edge split (heavy edges relaxed once per bucket)
 };
 
 // ctl->i32[k % 3]  size of the near queue processed by near iteration k
@@ -67,6 +73,8 @@ __global__ void __launch_bounds__(kThreads) sssp_persistent(SsspArgs a) {
     a.dist[v] = (v == a.src) ? 0 : kInf;
     a.stamp[v] = 0;
     a.farflag[v] = 0;
+    a.expanded[v] = kInf;
+    a.inmember[v] = 0;
   }
   if (gtid < kDeltaSamples && a.edges > 0) {
     const long long e = gtid * a.edges / kDeltaSamples;
@@ -95,71 +103,147 @@ __global__ void __launch_bounds__(kThreads) sssp_persistent(SsspArgs a) {
   long long T = delta;  // distances < T are near
   int it = 0;           // near iteration index (stamp it+1 marks the next queue)
   int epoch = 0;
+  int mpass = 0;        // heavy passes done
   long long improved = 0, frontier_v = 0, frontier_e = 0;
 
   while (true) {
     // ------------------------------------------------------------ near phase
-    while (cur_size > 0) {
-      // queue for iteration k: counter slot k % 3; iteration k appends to
-      // slot (k+1) % 3 and clears slot (k+2) % 3 (last read two iterations ago)
+    // Light passes expand the near queue and relax only edges lighter than
+    // delta (all edges when the split is off); every expanded vertex joins the
+    // member list.  When the near queue is empty, a heavy pass relaxes the
+    // heavy edges of the members once, with their settled distances (a heavy
+    // edge cannot improve a vertex of the same bucket).  Member count: slot
+    // 9 + mpass % 2; a heavy pass clears the other slot.
+    int nmem = 0;
+    while (cur_size > 0 || nmem > 0) {
+      const bool heavy = cur_size == 0;
       if (gtid == 0) {
         ctl->i32[(it + 2) % 3] = 0;
         ctl->i32[3 + (it + 1) % 3] = 0;
+        if (heavy) ctl->i32[9 + (mpass + 1) % 2] = 0;
       }
       int* qsize = &ctl->i32[(it + 1) % 3];
       int* nhub = &ctl->i32[3 + it % 3];
+      int* nmembers = &ctl->i32[9 + mpass % 2];
       int* far = (epoch & 1) ? a.fb : a.fa;
       int* fsize = &ctl->i32[6 + epoch % 3];
       const int next_stamp = it + 1;
       const int far_mark = epoch + 1;
+      const int* frontier = heavy ? a.members : cur;
+      const int fcount = heavy ? nmem : cur_size;
       auto relax = [&](bool act, int e, int du) {
         bool to_near = false, to_far = false;
         int v = 0;
         if (act && du != kInf) {
-          v = __ldg(&a.nlist[e]);
-          const long long nd = (long long)du + __ldg(&a.eweight[e]);
-          if (nd < (long long)a.dist[v]) {
-            const int ndi = (int)nd;
-            const int old = atomicMin(&a.dist[v], ndi);
-            if (ndi < old) {
-              improved++;
-              if (nd < T) to_near = atomicExch(&a.stamp[v], next_stamp) != next_stamp;
-              else to_far = atomicExch(&a.farflag[v], far_mark) != far_mark;
+          const int w = __ldg(&a.eweight[e]);
+          const bool light = !a.heavy_split || (long long)w < delta;
+          if (light != heavy) {
+            v = __ldg(&a.nlist[e]);
+            const long long nd = (long long)du + w;
+            if (nd < (long long)a.dist[v]) {
+              const int ndi = (int)nd;
+              const int old = atomicMin(&a.dist[v], ndi);
+              if (ndi < old) {
+                improved++;
+                if (nd < T) to_near = a.stamp[v] != next_stamp && atomicExch(&a.stamp[v], next_stamp) != next_stamp;
+                else to_far = a.farflag[v] != far_mark && atomicExch(&a.farflag[v], far_mark) != far_mark;
+              }
             }
           }
         }
         warp_append(to_near, v, nxt, qsize, a.nodes, ctl);
         warp_append(to_far, v, far, fsize, a.nodes, ctl);
       };
-      for (int base = warp_g * 32; base < cur_size; base += nwarps * 32) {
+      // Four edges per lane at a time: their loads, atomics and stamp checks
+      // are independent, so they are issued together.
+      auto relax4 = [&](const bool (&act)[4], const int (&e)[4], const int (&du)[4]) {
+        int v[4], w[4], dv[4], old[4];
+        bool cand[4];
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+          v[k] = 0;
+          w[k] = 0;
+          if (act[k] && du[k] != kInf) {
+            v[k] = __ldg(&a.nlist[e[k]]);
+            w[k] = __ldg(&a.eweight[e[k]]);
+          }
+        }
+#pragma unroll
+        for (int k = 0; k < 4; k++) dv[k] = (act[k] && du[k] != kInf) ? a.dist[v[k]] : 0;
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+          const bool light = !a.heavy_split || (long long)w[k] < delta;
+          cand[k] = act[k] && du[k] != kInf && light != heavy && (long long)du[k] + w[k] < (long long)dv[k];
+          old[k] = cand[k] ? atomicMin(&a.dist[v[k]], du[k] + w[k]) : 0;
+        }
+        int nq[4], fq[4];
+        int nn = 0, nf = 0;
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+          if (cand[k] && du[k] + w[k] < old[k]) {
+            improved++;
+            const long long nd = (long long)du[k] + w[k];
+            if (nd < T) {
+              if (a.stamp[v[k]] != next_stamp && atomicExch(&a.stamp[v[k]], next_stamp) != next_stamp)
+                nq[nn++] = v[k];
+            } else if (a.farflag[v[k]] != far_mark && atomicExch(&a.farflag[v[k]], far_mark) != far_mark) {
+              fq[nf++] = v[k];
+            }
+          }
+        }
+        warp_append_n<4>(nn, nq, nxt, qsize, a.nodes, ctl);
+        warp_append_n<4>(nf, fq, far, fsize, a.nodes, ctl);
+      };
+      for (int base = warp_g * 32; base < fcount; base += nwarps * 32) {
         const int i = base + lane;
         int u = 0, beg = 0, deg = 0, du = kInf;
-        if (i < cur_size) {
-          u = cur[i];
-          beg = __ldg(&a.nindex[u]);
-          deg = __ldg(&a.nindex[u + 1]) - beg;
+        bool expand = false;
+        if (i < fcount) {
+          u = frontier[i];
           du = a.dist[u];
+          if (heavy) {
+            a.inmember[u] = 0;
+            expand = true;
+          } else if (du < a.expanded[u]) {
+            // a vertex improved while already queued is queued again; expand
+            // it only if its distance dropped since its last expansion
+            a.expanded[u] = du;
+            expand = true;
+          }
+          if (expand) {
+            beg = __ldg(&a.nindex[u]);
+            deg = __ldg(&a.nindex[u + 1]) - beg;
+          }
         }
+        if (a.heavy_split && !heavy)
+          warp_append(expand && atomicExch(&a.inmember[u], 1) == 0, u, a.members, nmembers, a.nodes, ctl);
         const bool hub = deg > a.hub_degree;
         warp_append(hub, u, a.hubs, nhub, a.nodes, ctl);
-        if (i < cur_size) {
+        if (expand) {
           frontier_v++;
           frontier_e += deg;
         }
-        warp_expand(beg, hub ? 0 : deg, [&](bool act, int e, int j) {
-          const int duj = __shfl_sync(IG_FULL, du, j);
-          relax(act, e, duj);
+        warp_expand4(beg, hub ? 0 : deg, [&](const bool (&act)[4], const int (&e)[4], const int (&j)[4]) {
+          int duj[4];
+#pragma unroll
+          for (int k = 0; k < 4; k++) duj[k] = __shfl_sync(IG_FULL, du, j[k]);
+          relax4(act, e, duj);
         });
       }
       if (!grid_sync(ctl, a.timeout_ns)) return;
       const int nh = ld_relaxed(nhub);
       if (nh > 0) {
-        grid_expand_hubs(a.nindex, a.hubs, nh, [&](bool act, int e, int hv) {
-          relax(act, e, act ? a.dist[hv] : kInf);
+        grid_expand_hubs4(a.nindex, a.hubs, nh, [&](const bool (&act)[4], const int (&e)[4], const int (&hv)[4]) {
+          int duh[4];
+#pragma unroll
+          for (int k = 0; k < 4; k++) duh[k] = act[k] ? a.dist[hv[k]] : kInf;
+          relax4(act, e, duh);
         });
         if (!grid_sync(ctl, a.timeout_ns)) return;
       }
+      if (heavy) mpass++;
       cur_size = ld_relaxed(qsize);
+      nmem = a.heavy_split ? ld_relaxed(&ctl->i32[9 + mpass % 2]) : 0;
       it++;
       int* t = cur;
       cur = nxt;
@@ -239,11 +323,16 @@ int igk_sssp(IgExec* ex, const ig_csr* dg, int src, int* d_dist) {
   if ((rc = ig_scratch_get(ex->scratch, IG_SLOT_V0, vb, &stamp))) return rc;
   if ((rc = ig_scratch_get(ex->scratch, IG_SLOT_V1, vb, &farflag))) return rc;
   if ((rc = ig_scratch_get(ex->scratch, IG_SLOT_V2, vb, &hubs))) return rc;
+  void *expanded, *members, *inmember;
+  if ((rc = ig_scratch_get(ex->scratch, IG_SLOT_F0, vb, &expanded))) return rc;
+  if ((rc = ig_scratch_get(ex->scratch, IG_SLOT_F1, vb, &members))) return rc;
+  if ((rc = ig_scratch_get(ex->scratch, IG_SLOT_E0, vb, &inmember))) return rc;
   if ((rc = ig_exec_reset(ex))) return rc;
   const IgOptions& o = ig_options();
   SsspArgs a{dg->nindex, dg->nlist, dg->eweight, dg->nodes, dg->edges, src, d_dist,
              (int*)qa, (int*)qb, (int*)fa, (int*)fb, (int*)stamp, (int*)farflag, (int*)hubs,
-             ex->d_ctl, ex->timeout_ns, o.hub_degree, o.sssp_delta, o.sssp_delta_scale};
+             (int*)expanded, (int*)members, (int*)inmember, ex->d_ctl, ex->timeout_ns, o.hub_degree,
+             o.sssp_delta, o.sssp_delta_scale, o.sssp_heavy_split};
   void* args[] = {&a};
   return ig_launch_coop(ex, (const void*)sssp_persistent, kThreads, 0, o.blocks_per_sm, args, nullptr);
 }

@@ -216,10 +216,14 @@ __device__ __forceinline__ unsigned hash_slot(int w, unsigned mask) { return ((u
 // The warp hashes N+(v) into its shared-memory table, then walks the
 // out-lists N+(u) of the chunk's in-neighbours (load-balanced) and probes:
 // w in N+(u) and in N+(v) closes the triangle u -> v -> w, counted once at v.
+// kBatched: the graph is a disjoint union; triangles are added to the count of
+// the graph that holds their middle vertex (graph_vptr: first vertex of each graph).
+template <bool kBatched>
 __global__ void __launch_bounds__(kThreads) tc_count(const int* __restrict__ out_off, const int* __restrict__ out_list,
                                                      const int* __restrict__ nindex, const int* __restrict__ in_list,
                                                      const int* __restrict__ item_off, int n,
-                                                     unsigned long long* count, const IgCtl* ctl) {
+                                                     unsigned long long* count, const IgCtl* ctl,
+                                                     const int* __restrict__ graph_vptr, int graphs) {
   using namespace ig;
   extern __shared__ int s_tab[];
   if (ctl->err) return;
@@ -269,6 +273,7 @@ __global__ void __launch_bounds__(kThreads) tc_count(const int* __restrict__ out
     const int iend = __ldg(&nindex[v + 1]) - __ldg(&out_off[v + 1]);
     const int c0 = ib + (it - __ldg(&item_off[v])) * kChunk;
     const int c1 = min(c0 + kChunk, iend);
+    const unsigned long long before_item = local;
     for (int g = c0; g < c1; g += 32) {
       int ub = 0, ud = 0;
       if (g + lane < c1) {
@@ -308,7 +313,22 @@ __global__ void __launch_bounds__(kThreads) tc_count(const int* __restrict__ out
         }
       });
     }
+    if (kBatched) {
+      unsigned long long mine = local - before_item;
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) mine += __shfl_xor_sync(IG_FULL, mine, o);
+      if (lane == 0 && mine) {
+        int glo = 0, ghi = graphs - 1;  // graph of v: largest g with graph_vptr[g] <= v
+        while (glo < ghi) {
+          const int mid = (glo + ghi + 1) >> 1;
+          if (__ldg(&graph_vptr[mid]) <= v) glo = mid;
+          else ghi = mid - 1;
+        }
+        atomicAdd(&count[glo], mine);
+      }
+    }
   }
+  if (kBatched) return;
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) local += __shfl_xor_sync(IG_FULL, local, o);
   if (lane == 0 && local) atomicAdd(count, local);
@@ -316,7 +336,20 @@ __global__ void __launch_bounds__(kThreads) tc_count(const int* __restrict__ out
 
 }  // namespace
 
+static int tc_run(IgExec* ex, int nodes, int edges, const int* d_nindex, const int* d_nlist, unsigned long long* d_count,
+                  const int* d_graph_vptr, int graphs);
+
 int igk_tc(IgExec* ex, int nodes, int edges, const int* d_nindex, const int* d_nlist, unsigned long long* d_count) {
+  return tc_run(ex, nodes, edges, d_nindex, d_nlist, d_count, nullptr, 0);
+}
+
+int igk_tc_batched(IgExec* ex, int nodes, int edges, const int* d_nindex, const int* d_nlist,
+                   const int* d_graph_vptr, int graphs, unsigned long long* d_counts) {
+  return tc_run(ex, nodes, edges, d_nindex, d_nlist, d_counts, d_graph_vptr, graphs);
+}
+
+static int tc_run(IgExec* ex, int nodes, int edges, const int* d_nindex, const int* d_nlist, unsigned long long* d_count,
+                  const int* d_graph_vptr, int graphs) {
   const size_t vb = ((size_t)nodes + 1) * sizeof(int);
   void *cnt, *off, *icnt, *ioff, *list, *inl, *hubs;
   int rc;
@@ -330,16 +363,19 @@ int igk_tc(IgExec* ex, int nodes, int edges, const int* d_nindex, const int* d_n
   if ((rc = ig_scratch_get(ex->scratch, IG_SLOT_G1, std::max<size_t>(1, (size_t)edges) * sizeof(int), &inl)))
     return rc;
   if ((rc = ig_exec_reset(ex))) return rc;
-  if ((rc = ig_cuda_check((int)cudaMemsetAsync(d_count, 0, sizeof(unsigned long long), ex->stream), "memset")))
+  const size_t ncount = d_graph_vptr ? (size_t)graphs : 1;
+  if ((rc = ig_cuda_check((int)cudaMemsetAsync(d_count, 0, ncount * sizeof(unsigned long long), ex->stream),
+                          "memset")))
     return rc;
-  static bool attr_set[64] = {};
+  static bool attr_set[2][64] = {};
   const size_t smem = (size_t)kWarps * (kHashCap + kBitWords) * sizeof(int);
-  if (ex->device >= 0 && ex->device < 64 && !attr_set[ex->device]) {
-    if ((rc = ig_cuda_check((int)cudaFuncSetAttribute((const void*)tc_count,
-                                                      cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
+  const int bi = d_graph_vptr ? 1 : 0;
+  if (ex->device >= 0 && ex->device < 64 && !attr_set[bi][ex->device]) {
+    const void* fn = d_graph_vptr ? (const void*)tc_count<true> : (const void*)tc_count<false>;
+    if ((rc = ig_cuda_check((int)cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
                             "tc smem attribute")))
       return rc;
-    attr_set[ex->device] = true;
+    attr_set[bi][ex->device] = true;
   }
   const int grid = std::max(1, std::min((nodes + kThreads - 1) / kThreads, ex->sms * 8));
   tc_orient_count<<<grid, kThreads, 0, ex->stream>>>(d_nindex, d_nlist, nodes, (int*)cnt, (int*)icnt, (int*)hubs,
@@ -352,9 +388,14 @@ int igk_tc(IgExec* ex, int nodes, int edges, const int* d_nindex, const int* d_n
                                                      (int*)inl, ex->d_ctl);
   tc_orient_hubs_fill<<<ex->sms * 8, kThreads, 0, ex->stream>>>(d_nindex, d_nlist, (const int*)hubs,
                                                                 (const int*)off, (int*)list, (int*)inl, ex->d_ctl);
-  tc_count<<<ex->sms * 3, kThreads, smem, ex->stream>>>((const int*)off, (const int*)list, d_nindex,
-                                                        (const int*)inl, (const int*)ioff, nodes, d_count,
-                                                        ex->d_ctl);
+  if (d_graph_vptr)
+    tc_count<true><<<ex->sms * 3, kThreads, smem, ex->stream>>>((const int*)off, (const int*)list, d_nindex,
+                                                                (const int*)inl, (const int*)ioff, nodes, d_count,
+                                                                ex->d_ctl, d_graph_vptr, graphs);
+  else
+    tc_count<false><<<ex->sms * 3, kThreads, smem, ex->stream>>>((const int*)off, (const int*)list, d_nindex,
+                                                                 (const int*)inl, (const int*)ioff, nodes, d_count,
+                                                                 ex->d_ctl, nullptr, 0);
   ig_count_launches(5);
   return ig_cuda_check((int)cudaGetLastError(), "tc launch");
 }

@@ -12,4 +12,6 @@ from .dropin import (GPUbfs_edge, GPUbfs_vertex, GPUcc_edge, GPUcc_vertex, GPUmi
 from .device import (DeviceGraph, Event, create_stream, get_option, kernel_launches, set_option,  # noqa: F401
                      set_wait_timeout_ms)
 
+from .batch import Batch, gen_batch, pack, unpack  # noqa: F401
+
 INT_MAX = 2147483647

@@ -125,6 +125,17 @@ SIGNATURES = {
     "ig_graph_set_stream": (_I, [_P, _P]),
     "ig_kernel_launches": (_I, [ctypes.POINTER(ctypes.c_longlong)]),
     "ig_bfs_vertex_noalloc": (_I, [_I, _PCSR, _P, _P]),
+    "ig_batch_create": (_I, [_PCSR, _P, _I, ctypes.POINTER(_P)]),
+    "ig_batch_destroy": (_I, [_P]),
+    "ig_batch_stream": (_I, [_P, ctypes.POINTER(_P)]),
+    "ig_batch_use_graphs": (_I, [_P, _I]),
+    "ig_batch_last_run": (_I, [_P, ctypes.POINTER(RunInfo)]),
+    "ig_batch_bfs": (_I, [_P, _P, _P]),
+    "ig_batch_cc": (_I, [_P, _P]),
+    "ig_batch_tc": (_I, [_P, _P]),
+    "ig_batch_pagerank": (_I, [_P, _P, ctypes.c_float, _I, _P]),
+    "ig_gen_batch": (_I, [_I, _I, _I, ctypes.c_double, _I, ctypes.c_double, ctypes.c_double, ctypes.c_double, _U64,
+                          _I, _PCSR, _P]),
 }
 
 _lib = None

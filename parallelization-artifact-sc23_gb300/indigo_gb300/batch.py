@@ -1,0 +1,108 @@
+"""Batched form: many graphs packed as one disjoint union with global vertex
+ids plus graph_vptr (first vertex of each graph), processed by one launch
+sequence per algorithm (ig_batch_*), captured into a CUDA graph after its
+first call."""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+
+from ._lib import CSR, RunInfo, check, load
+from .graph import DeviceBuffer, DeviceCSR, Graph, _take_csr
+
+
+def pack(graphs: list) -> tuple:
+    """Disjoint union of host graphs -> (union Graph, vptr int32[len+1])."""
+    vptr = np.zeros(len(graphs) + 1, np.int64)
+    eptr = np.zeros(len(graphs) + 1, np.int64)
+    for i, g in enumerate(graphs):
+        vptr[i + 1] = vptr[i] + g.nodes
+        eptr[i + 1] = eptr[i] + g.edges
+    if vptr[-1] > 2**31 - 1 or eptr[-1] > 2**31 - 1:
+        raise ValueError("batch exceeds int32 vertex or edge ids")
+    nindex = np.concatenate([g.nindex[:-1].astype(np.int64) + eptr[i] for i, g in enumerate(graphs)] +
+                            [np.array([eptr[-1]])]).astype(np.int32)
+    nlist = np.concatenate([g.nlist.astype(np.int64) + vptr[i] for i, g in enumerate(graphs)]).astype(np.int32) \
+        if eptr[-1] else np.zeros(0, np.int32)
+    ew = None
+    if all(g.eweight is not None for g in graphs):
+        ew = np.concatenate([g.eweight for g in graphs]).astype(np.int32) if eptr[-1] else np.zeros(0, np.int32)
+    return Graph(nindex, nlist, ew), vptr.astype(np.int32)
+
+
+def unpack(union: Graph, vptr: np.ndarray, i: int) -> Graph:
+    """Graph i of a packed union, with local ids."""
+    v0, v1 = int(vptr[i]), int(vptr[i + 1])
+    e0, e1 = int(union.nindex[v0]), int(union.nindex[v1])
+    nindex = union.nindex[v0:v1 + 1] - e0
+    nlist = union.nlist[e0:e1] - v0
+    ew = union.eweight[e0:e1] if union.eweight is not None else None
+    return Graph(nindex, nlist, ew)
+
+
+def gen_batch(graphs: int, vmin: int = 1024, vmax: int = 65536, er_degree: float = 8.0, rmat_edge_factor: int = 8,
+              a: float = 0.57, b: float = 0.19, c: float = 0.19, seed: int = 13, maxw: int = 255) -> tuple:
+    """Host generator of a batch (even: Erdos-Renyi, odd: RMAT) -> (union, vptr)."""
+    out = CSR()
+    vptr = np.empty(graphs + 1, np.int32)
+    check(load().ig_gen_batch(graphs, vmin, vmax, er_degree, rmat_edge_factor, a, b, c, seed, maxw,
+                              ctypes.byref(out), vptr.ctypes.data_as(ctypes.c_void_p)))
+    return _take_csr(out), vptr
+
+
+class Batch:
+    def __init__(self, union: Graph, vptr: np.ndarray):
+        self.union = union
+        self.vptr = np.ascontiguousarray(vptr, dtype=np.int32)
+        self.graphs = len(self.vptr) - 1
+        self.nodes = union.nodes
+        self.d = DeviceCSR(union)
+        self.d_vptr = DeviceBuffer.from_array(self.vptr)
+        h = ctypes.c_void_p()
+        check(load().ig_batch_create(ctypes.byref(self.d.c), self.d_vptr.ptr, self.graphs, ctypes.byref(h)))
+        self.h = h.value
+        s = ctypes.c_void_p()
+        check(load().ig_batch_stream(self.h, ctypes.byref(s)))
+        self.stream = s.value
+
+    def use_graphs(self, enable: bool):
+        check(load().ig_batch_use_graphs(self.h, 1 if enable else 0))
+
+    def bfs(self, dist: DeviceBuffer, sources: DeviceBuffer | None = None):
+        check(load().ig_batch_bfs(self.h, sources.ptr if sources is not None else None, dist.ptr))
+
+    def cc(self, label: DeviceBuffer):
+        check(load().ig_batch_cc(self.h, label.ptr))
+
+    def tc(self, counts: DeviceBuffer):
+        check(load().ig_batch_tc(self.h, counts.ptr))
+
+    def pagerank(self, scores: DeviceBuffer, epsilon: float, max_iter: int, iters: DeviceBuffer):
+        check(load().ig_batch_pagerank(self.h, scores.ptr, epsilon, max_iter, iters.ptr))
+
+    def last_run(self) -> RunInfo:
+        info = RunInfo()
+        check(load().ig_batch_last_run(self.h, ctypes.byref(info)))
+        return info
+
+    def synchronize(self):
+        check(load().ig_stream_synchronize(self.stream))
+
+    def close(self):
+        if getattr(self, "h", None):
+            load().ig_batch_destroy(self.h)
+            self.h = None
+            self.d.close()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
