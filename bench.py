@@ -593,6 +593,109 @@ def run_batched(args, dist: Dist):
             "speedup_vs_plain": round(value / plain_value, 1), "clocks": clk, "gpu_launches": launches}
 
 
+# ----------------------------------------------------------------------------- served form
+SERVE_SCALE, SERVE_SEED = 24, 17
+SERVE_RATES = [1000, 3000, 10000, 30000, 100000]
+
+
+def run_served(args, dist: Dist):
+    """Configuration 5: resident RMAT-24 (seed 17, weights [1, 1000]); Poisson
+    arrivals of single-source BFS and SSSP queries (sources uniform over
+    vertices with degree > 0, 4 random targets each) at each offered rate;
+    each query's latency runs from submission to its answer on the host.
+    The plain comparison answers queries one at a time with the drop-in calls."""
+    import threading
+
+    import indigo_gb300 as ig
+
+    ig.check(ig.load().ig_set_device(dist.local))
+    t0 = time.time()
+    g = ig.rmat(args.serve_scale, 16, 0.57, 0.19, 0.19, seed=SERVE_SEED, maxw=1000)
+    log(f"[bench] served graph RMAT-{args.serve_scale}: V={g.nodes} E={g.edges} in {time.time() - t0:.1f}s")
+    d = ig.DeviceCSR(g)
+    rng = np.random.default_rng(SERVE_SEED)
+    pool = g.pick_sources(4096, seed=SERVE_SEED)
+    srv = ig.Server(d, max_pending=1 << 16)
+    # warm-up: one of each
+    for k in (0, 1):
+        srv.wait(srv.submit(k, int(pool[0])), 600000)
+    per_kind = {}
+    clocks = ClockSampler(dist.local)
+    for kind, name in ((0, "bfs"), (1, "sssp")):
+        rows = []
+        for rate in SERVE_RATES:
+            n = int(min(args.serve_queries, max(64, rate * args.serve_seconds)))
+            gaps = rng.exponential(1.0 / rate, n)
+            srcs = rng.choice(pool, n)
+            tickets = [None] * n
+            rejected = [0]
+
+            def client():
+                t_next = time.perf_counter()
+                for i in range(n):
+                    t_next += gaps[i]
+                    while True:
+                        now = time.perf_counter()
+                        if now >= t_next:
+                            break
+                        if t_next - now > 2e-4:
+                            time.sleep(t_next - now - 1e-4)
+                    t = srv.try_submit(kind, int(srcs[i]), rng.integers(0, g.nodes, 4))
+                    if t is None:
+                        rejected[0] += 1
+                    tickets[i] = t
+
+            th = threading.Thread(target=client)
+            w0 = time.perf_counter()
+            th.start()
+            th.join()
+            lat = []
+            last_done = 0.0
+            first_submit = None
+            for t in tickets:
+                if t is None:
+                    continue
+                a = srv.wait(t, 600000)
+                lat.append(a.latency_s)
+            wall = time.perf_counter() - w0
+            lat = np.array(lat) if lat else np.array([float("nan")])
+            rows.append({"offered_qps": rate, "queries": n, "rejected": rejected[0],
+                         "achieved_qps": round(len(lat) / wall, 1),
+                         "p50_ms": round(1e3 * float(np.percentile(lat, 50)), 3),
+                         "p99_ms": round(1e3 * float(np.percentile(lat, 99)), 3)})
+            log(f"[bench] served {name} @ {rate}/s: {rows[-1]}")
+        # plain: one drop-in call per query, one after another
+        m = args.plain_queries
+        out = np.empty(g.nodes, np.int32)
+        fn = ig.GPUbfs_vertex if kind == 0 else ig.GPUsssp_vertex
+        fn(int(pool[1]), d, out)
+        ptimes = []
+        for i in range(m):
+            t1 = time.perf_counter()
+            fn(int(pool[2 + i]), d, out)
+            ig.summarize(kind, int(pool[2 + i]), out, [0, 1, 2, 3])
+            ptimes.append(time.perf_counter() - t1)
+        ptimes = np.array(ptimes)
+        best = max(rows, key=lambda r: r["achieved_qps"])
+        per_kind[name] = {"rates": rows, "best_achieved_qps": best["achieved_qps"],
+                          "plain_qps": round(1.0 / float(ptimes.mean()), 1),
+                          "plain_p50_ms": round(1e3 * float(np.percentile(ptimes, 50)), 3),
+                          "plain_p99_ms": round(1e3 * float(np.percentile(ptimes, 99)), 3),
+                          "speedup_vs_plain": round(best["achieved_qps"] * float(ptimes.mean()), 1)}
+    clk = clocks.stop()
+    srv.close()
+    d.close()
+    value = sum(v["best_achieved_qps"] for v in per_kind.values())
+    return {"metric": "served queries/s (RMAT-24, BFS and SSSP, Poisson arrivals) with p50/p99 latency",
+            "value": round(value, 1), "unit": "queries/s", "n_gpus": dist.world, "steps": len(SERVE_RATES),
+            "warmup": 1, "ms_per_step": None, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "int32", "data": "synthetic",
+            "config": {"workload": f"served_rmat{args.serve_scale}", "vertices": g.nodes, "edges": g.edges,
+                       "lanes_per_engine": 64, "rates": SERVE_RATES, "targets_per_query": 4,
+                       "l2": "resident graph larger than L2"},
+            "per_kind": per_kind, "clocks": clk}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -601,8 +704,13 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--form", choices=["plain", "batched"], default="plain",
-                    help="plain: the six algorithms on RMAT-22 (default); batched: 4096 packed graphs")
+    ap.add_argument("--form", choices=["plain", "batched", "served"], default="plain",
+                    help="plain: the six algorithms on RMAT-22 (default); batched: 4096 packed graphs; "
+                         "served: queries against resident RMAT-24")
+    ap.add_argument("--serve-scale", type=int, default=SERVE_SCALE)
+    ap.add_argument("--serve-seconds", type=float, default=1.0, help="offered-load duration per rate")
+    ap.add_argument("--serve-queries", type=int, default=3000, help="cap on queries per rate")
+    ap.add_argument("--plain-queries", type=int, default=16)
     ap.add_argument("--plain-sample", type=int, default=256, help="graphs timed with plain calls (batched form)")
     args = ap.parse_args()
     if args.warmup < 3:
@@ -616,6 +724,8 @@ def main():
             out = run_reference(args, dist)
         elif args.form == "batched":
             out = run_batched(args, dist)
+        elif args.form == "served":
+            out = run_served(args, dist)
         else:
             out = run_ours(args, dist)
         if dist.rank == 0:

@@ -277,6 +277,41 @@ int ig_gen_batch(int graphs, int vmin, int vmax, double er_degree, int rmat_edge
                  double c, uint64_t seed, int maxw, ig_csr* out_union, int* out_vptr);
 
 /* ---------------------------------------------------------------------------
+ * Served form: BFS / SSSP queries against a resident graph (no counterpart
+ * in the reference).  A worker thread answers them with 64-lane multi-source
+ * traversals; queries join free lanes at every step and leave when done
+ * (continuous batching).  A query returns summary results, not the full
+ * distance vector: vertices reached, the largest finite distance, the sum of
+ * the finite distances and the distances to up to 16 requested targets.
+ * ------------------------------------------------------------------------ */
+typedef struct ig_server ig_server;
+typedef struct ig_query_result {
+  int status;              /* IG_OK or the failure of the serving worker */
+  int kind;                /* 0 BFS, 1 SSSP */
+  int source;
+  int levels;              /* BFS: max_dist + 1; SSSP: rounds the engine ran */
+  long long reached;       /* vertices reached, the source included */
+  long long max_dist;      /* largest finite distance */
+  long long sum_dist;      /* sum of the finite distances */
+  int ntargets;
+  int targets[16];
+  int target_dist[16];     /* INT_MAX: unreachable */
+  double submit_time;      /* seconds, steady clock */
+  double admit_time;
+  double done_time;
+} ig_query_result;
+/* d_g: device graph (eweight needed for SSSP queries); the graph stays
+ * resident and caller-owned.  max_pending bounds the admission queue.
+ * Fails with IG_ERR_NOMEM when the engines' state does not fit in free
+ * device memory. */
+int ig_server_create(const ig_csr* d_g, int max_pending, ig_server** out);
+/* kind 0 BFS, 1 SSSP; IG_ERR_BUSY when max_pending queries are waiting. */
+int ig_server_submit(ig_server* s, int kind, int source, const int* targets, int ntargets, long long* ticket);
+int ig_server_wait(ig_server* s, long long ticket, int timeout_ms, ig_query_result* out);
+int ig_server_stats(ig_server* s, long long* completed, long long* steps);
+int ig_server_destroy(ig_server* s);
+
+/* ---------------------------------------------------------------------------
  * Self-test (no counterpart in the reference, whose waits are host-side)
  * ------------------------------------------------------------------------ */
 /* Launches a persistent kernel in which one block never reaches the grid

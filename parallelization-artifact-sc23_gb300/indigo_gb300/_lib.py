@@ -44,6 +44,26 @@ class CSR(ctypes.Structure):
     ]
 
 
+class QueryResult(ctypes.Structure):
+    """struct ig_query_result."""
+
+    _fields_ = [
+        ("status", ctypes.c_int),
+        ("kind", ctypes.c_int),
+        ("source", ctypes.c_int),
+        ("levels", ctypes.c_int),
+        ("reached", ctypes.c_longlong),
+        ("max_dist", ctypes.c_longlong),
+        ("sum_dist", ctypes.c_longlong),
+        ("ntargets", ctypes.c_int),
+        ("targets", ctypes.c_int * 16),
+        ("target_dist", ctypes.c_int * 16),
+        ("submit_time", ctypes.c_double),
+        ("admit_time", ctypes.c_double),
+        ("done_time", ctypes.c_double),
+    ]
+
+
 class RunInfo(ctypes.Structure):
     _fields_ = [
         ("status", ctypes.c_int),
@@ -134,6 +154,11 @@ SIGNATURES = {
     "ig_batch_cc": (_I, [_P, _P]),
     "ig_batch_tc": (_I, [_P, _P]),
     "ig_batch_pagerank": (_I, [_P, _P, ctypes.c_float, _I, _P]),
+    "ig_server_create": (_I, [_PCSR, _I, ctypes.POINTER(_P)]),
+    "ig_server_submit": (_I, [_P, _I, _I, _P, _I, ctypes.POINTER(ctypes.c_longlong)]),
+    "ig_server_wait": (_I, [_P, ctypes.c_longlong, _I, ctypes.POINTER(QueryResult)]),
+    "ig_server_stats": (_I, [_P, ctypes.POINTER(ctypes.c_longlong), ctypes.POINTER(ctypes.c_longlong)]),
+    "ig_server_destroy": (_I, [_P]),
     "ig_gen_batch": (_I, [_I, _I, _I, ctypes.c_double, _I, ctypes.c_double, ctypes.c_double, ctypes.c_double, _U64,
                           _I, _PCSR, _P]),
 }
