@@ -686,7 +686,7 @@ def run_served(args, dist: Dist):
     srv.close()
     d.close()
     value = sum(v["best_achieved_qps"] for v in per_kind.values())
-    return {"metric": "served queries/s (RMAT-24, BFS and SSSP, Poisson arrivals) with p50/p99 latency",
+    return {"metric": f"served queries/s (RMAT-{args.serve_scale}, BFS and SSSP, Poisson arrivals) with p50/p99 latency",
             "value": round(value, 1), "unit": "queries/s", "n_gpus": dist.world, "steps": len(SERVE_RATES),
             "warmup": 1, "ms_per_step": None, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "int32", "data": "synthetic",
