@@ -69,11 +69,17 @@ class Dist:
             self.td.barrier()
 
     def max(self, x: float) -> float:
+        return self._reduce(x, "MAX")
+
+    def sum(self, x: float) -> float:
+        return self._reduce(x, "SUM")
+
+    def _reduce(self, x: float, op: str) -> float:
         if self.world == 1:
             return x
         import torch
         t = torch.tensor([x], dtype=torch.float64)
-        self.td.all_reduce(t, op=self.td.ReduceOp.MAX)
+        self.td.all_reduce(t, op=getattr(self.td.ReduceOp, op))
         return float(t.item())
 
     def close(self):
@@ -501,14 +507,26 @@ def run_batched(args, dist: Dist):
     even Erdos-Renyi with average degree 8, odd RMAT with edge factor 8,
     weights in [1, 255], seed 13).  One step = CC, BFS from vertex 0, TC and
     PageRank of every graph with one batched call each (CUDA-graph replay);
-    value = graphs/s.  The plain comparison runs the same four algorithms as
-    one drop-in call per graph and algorithm (a sample of the graphs, scaled)."""
+    value = graphs/s over all ranks.  With N ranks the graphs shard with no
+    exchange: "weak" gives every rank its own pack of 4096 graphs (seed 13 +
+    rank), "strong" gives each rank an edge-balanced contiguous slice of the
+    one pack.  The plain comparison runs the same four algorithms as one
+    drop-in call per graph and algorithm (a sample of the graphs, scaled)."""
     import indigo_gb300 as ig
 
     ig.check(ig.load().ig_set_device(dist.local))
     t0 = time.time()
-    u, vptr = ig.gen_batch(BATCH_GRAPHS, BATCH_VMIN, BATCH_VMAX, 8.0, 8, 0.57, 0.19, 0.19, BATCH_SEED, 255)
-    log(f"[bench] batch: {BATCH_GRAPHS} graphs, V={u.nodes} E={u.edges}, generated in {time.time() - t0:.1f}s")
+    strong = dist.world > 1 and args.batch_split == "strong"
+    seed = BATCH_SEED + (0 if strong else dist.rank)
+    u, vptr = ig.gen_batch(BATCH_GRAPHS, BATCH_VMIN, BATCH_VMAX, 8.0, 8, 0.57, 0.19, 0.19, seed, 255)
+    if strong:
+        g0, g1 = ig.split_batch(u, vptr, dist.world)[dist.rank]
+        if g1 <= g0:
+            raise RuntimeError(f"rank {dist.rank} received no graphs")
+        u, vptr = ig.take_batch(u, vptr, g0, g1)
+    graphs_here = len(vptr) - 1
+    log(f"[bench] batch (rank {dist.rank}): {graphs_here} graphs, V={u.nodes} E={u.edges}, "
+        f"generated in {time.time() - t0:.1f}s")
     b = ig.Batch(u, vptr)
     V = u.nodes
     d_dist, d_lab = ig.DeviceBuffer(4 * V), ig.DeviceBuffer(4 * V)
@@ -559,11 +577,12 @@ def run_batched(args, dist: Dist):
     if b.last_run().status:
         raise RuntimeError("batched run failed during timing")
     ms = dist.max(t_a.elapsed_ms(t_b)) / args.steps
-    value = dist.world * BATCH_GRAPHS / (ms * 1e-3)
+    graphs_all = int(dist.sum(graphs_here))
+    value = graphs_all / (ms * 1e-3)
 
     # plain drop-in calls, one per graph and algorithm, on a sample of graphs
     rng = np.random.default_rng(BATCH_SEED)
-    sample = np.sort(rng.choice(BATCH_GRAPHS, size=min(args.plain_sample, BATCH_GRAPHS), replace=False))
+    sample = np.sort(rng.choice(graphs_here, size=min(args.plain_sample, graphs_here), replace=False))
     plain_s = 0.0
     for i in sample:
         g = ig.unpack(u, vptr, int(i))
@@ -582,9 +601,12 @@ def run_batched(args, dist: Dist):
     b.close()
     return {"metric": "graphs/s (4096 packed graphs: CC + BFS + TC + PR per graph)", "value": round(value, 1),
             "unit": "graphs/s", "n_gpus": dist.world, "steps": args.steps, "warmup": args.warmup,
-            "ms_per_step": round(ms, 3), "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-            "dtype": "int32/f32", "data": "synthetic",
-            "config": {"workload": "batch4096_er8_rmat8", "graphs": BATCH_GRAPHS, "vertices": V, "edges": u.edges,
+            "ms_per_step": round(ms, 3), "higher_is_better": True, "scaling": "strong" if strong else "weak",
+            "vs_baseline": None, "dtype": "int32/f32", "data": "synthetic",
+            "config": {"workload": "batch4096_er8_rmat8", "graphs": graphs_all, "graphs_per_rank": graphs_here,
+                       "vertices": V, "edges": u.edges,
+                       "parallelism": (f"{dist.world} ranks, " + ("edge-balanced slices of one pack" if strong
+                                       else "one pack per rank")) if dist.world > 1 else "single GPU",
                        "vmin": BATCH_VMIN, "vmax": BATCH_VMAX, "seed": BATCH_SEED,
                        "l2": "inputs larger than L2 (%.0f MB neighbour lists)" % (4 * u.edges / 1e6)},
             "per_algo_ms": {k: round(v / args.steps, 3) for k, v in acc.items()},
@@ -685,7 +707,7 @@ def run_served(args, dist: Dist):
     clk = clocks.stop()
     srv.close()
     d.close()
-    value = sum(v["best_achieved_qps"] for v in per_kind.values())
+    value = dist.sum(sum(v["best_achieved_qps"] for v in per_kind.values()))  # one replica per rank
     return {"metric": f"served queries/s (RMAT-{args.serve_scale}, BFS and SSSP, Poisson arrivals) with p50/p99 latency",
             "value": round(value, 1), "unit": "queries/s", "n_gpus": dist.world, "steps": len(SERVE_RATES),
             "warmup": 1, "ms_per_step": None, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
@@ -708,6 +730,8 @@ def main():
                     help="plain: the six algorithms on RMAT-22 (default); batched: 4096 packed graphs; "
                          "served: queries against resident RMAT-24")
     ap.add_argument("--serve-scale", type=int, default=SERVE_SCALE)
+    ap.add_argument("--batch-split", choices=["weak", "strong"], default="weak",
+                    help="batched form with N ranks: a pack per rank (weak) or slices of one pack (strong)")
     ap.add_argument("--serve-seconds", type=float, default=1.0, help="offered-load duration per rate")
     ap.add_argument("--serve-queries", type=int, default=3000, help="cap on queries per rate")
     ap.add_argument("--plain-queries", type=int, default=16)

@@ -13,6 +13,7 @@ from .device import (DeviceGraph, Event, create_stream, get_option, kernel_launc
                      set_wait_timeout_ms)
 
 from .batch import Batch, gen_batch, pack, unpack  # noqa: F401
+from .batch import split as split_batch, take as take_batch  # noqa: F401
 from .serve import Answer, Server, summarize  # noqa: F401
 
 INT_MAX = 2147483647

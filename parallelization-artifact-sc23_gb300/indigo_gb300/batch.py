@@ -41,6 +41,39 @@ def unpack(union: Graph, vptr: np.ndarray, i: int) -> Graph:
     return Graph(nindex, nlist, ew)
 
 
+def split(union: Graph, vptr: np.ndarray, parts: int) -> list:
+    """Contiguous ranges of graphs, one per part, with about equal edge
+    counts (vertices break ties for edgeless packs): [(g0, g1), ...].  Used to
+    spread one pack over several GPUs; graphs are independent, so no exchange
+    between the parts is needed.  Part k starts at the first graph whose
+    cumulative work reaches k/parts of the total."""
+    if parts < 1:
+        raise ValueError("parts must be >= 1")
+    vptr = np.asarray(vptr, dtype=np.int64)
+    graphs = len(vptr) - 1
+    eptr = union.nindex.astype(np.int64)[vptr]
+    work = (eptr[1:] - eptr[:-1]) + (vptr[1:] - vptr[:-1])  # edges + vertices per graph
+    cum = np.concatenate([[0], np.cumsum(work)])
+    total = int(cum[-1])
+    bounds = [0]
+    for k in range(1, parts):
+        b = int(np.searchsorted(cum, total * k / parts, side="left"))
+        bounds.append(min(max(b, bounds[-1]), graphs))
+    bounds.append(graphs)
+    return [(bounds[k], bounds[k + 1]) for k in range(parts)]
+
+
+def take(union: Graph, vptr: np.ndarray, g0: int, g1: int) -> tuple:
+    """Graphs [g0, g1) of a packed union as their own union (ids re-based)."""
+    vptr = np.asarray(vptr, dtype=np.int64)
+    v0, v1 = int(vptr[g0]), int(vptr[g1])
+    e0, e1 = int(union.nindex[v0]), int(union.nindex[v1])
+    nindex = (union.nindex[v0:v1 + 1].astype(np.int64) - e0).astype(np.int32)
+    nlist = (union.nlist[e0:e1].astype(np.int64) - v0).astype(np.int32)
+    ew = union.eweight[e0:e1].copy() if union.eweight is not None else None
+    return Graph(nindex, nlist, ew), (vptr[g0:g1 + 1] - v0).astype(np.int32)
+
+
 def gen_batch(graphs: int, vmin: int = 1024, vmax: int = 65536, er_degree: float = 8.0, rmat_edge_factor: int = 8,
               a: float = 0.57, b: float = 0.19, c: float = 0.19, seed: int = 13, maxw: int = 255) -> tuple:
     """Host generator of a batch (even: Erdos-Renyi, odd: RMAT) -> (union, vptr)."""
