@@ -557,6 +557,14 @@ def run_batched(args, dist: Dist):
             for k in ev:
                 acc[k] += ev[k][0].elapsed_ms(ev[k][1])
 
+    tuned = None
+    if not args.no_autotune:
+        t1 = time.time()
+        tune_ms = b.autotune(("bfs", "cc", "pr"), reps=2)
+        tuned = {a: {"ms": round(tune_ms[a], 3),
+                     "options": {k: b.get_option(a, k) for k in ("blocks_per_sm", "hub_degree", "pr_hub_degree")}}
+                 for a in tune_ms}
+        log(f"[bench] autotuned in {time.time() - t1:.1f}s: {tuned}")
     for _ in range(args.warmup):
         step(False)
     if b.last_run().status:
@@ -610,6 +618,7 @@ def run_batched(args, dist: Dist):
                        "vmin": BATCH_VMIN, "vmax": BATCH_VMAX, "seed": BATCH_SEED,
                        "l2": "inputs larger than L2 (%.0f MB neighbour lists)" % (4 * u.edges / 1e6)},
             "per_algo_ms": {k: round(v / args.steps, 3) for k, v in acc.items()},
+            "autotuned": tuned,
             "plain": {"value": round(plain_value, 1), "unit": "graphs/s", "sample_graphs": int(len(sample)),
                       "api": "drop-in C ABI, one call per graph and algorithm (host wall clock, results to host)"},
             "speedup_vs_plain": round(value / plain_value, 1), "clocks": clk, "gpu_launches": launches}
@@ -730,6 +739,7 @@ def main():
                     help="plain: the six algorithms on RMAT-22 (default); batched: 4096 packed graphs; "
                          "served: queries against resident RMAT-24")
     ap.add_argument("--serve-scale", type=int, default=SERVE_SCALE)
+    ap.add_argument("--no-autotune", action="store_true", help="batched form: keep the process-wide options")
     ap.add_argument("--batch-split", choices=["weak", "strong"], default="weak",
                     help="batched form with N ranks: a pack per rank (weak) or slices of one pack (strong)")
     ap.add_argument("--serve-seconds", type=float, default=1.0, help="offered-load duration per rate")

@@ -268,6 +268,16 @@ int ig_batch_tc(ig_batch* b, unsigned long long* d_counts);
 /* PageRank of every graph with its own (1-d)/V_g and its own stop rule;
  * d_scores in/out by global vertex; d_iters[g] receives the iterations. */
 int ig_batch_pagerank(ig_batch* b, float* d_scores, float epsilon, int max_iter, int* d_iters);
+/* Autotuning of the batched form (no reference counterpart): for each
+ * algorithm in algo_mask (bit 0 BFS, 1 CC, 2 TC, 3 PageRank) times a small set
+ * of launch variants on this batch (blocks per SM, grid-expansion thresholds;
+ * never a change of results), best of `reps` runs each, and keeps the fastest
+ * for the batch's later calls.  best_ms[4] (may be NULL) receives the chosen
+ * variant's time per algorithm (-1 where not tuned).  Synchronous. */
+int ig_batch_autotune(ig_batch* b, int algo_mask, int reps, float* best_ms);
+/* The option value the batch uses for `algo` (0..3): the tuned one, else the
+ * process-wide value (names as in ig_get_option). */
+int ig_batch_get_option(ig_batch* b, int algo, const char* name, long long* value);
 /* Host generator of a batch: `graphs` graphs with vertex counts log-uniform
  * in [vmin, vmax]; even indices Erdos-Renyi (average degree er_degree), odd
  * ones RMAT (a, b, c; rmat_edge_factor pairs per vertex, ids taken modulo the

@@ -175,7 +175,7 @@ int igk_bfs(IgExec* ex, const ig_csr* dg, int src, int* d_dist) {
   if ((rc = ig_scratch_get(ex->scratch, IG_SLOT_Q1, vb, &qb))) return rc;
   if ((rc = ig_scratch_get(ex->scratch, IG_SLOT_Q2, vb, &hubs))) return rc;
   if ((rc = ig_exec_reset(ex))) return rc;
-  const IgOptions& o = ig_options();
+  const IgOptions& o = ig_exec_options(ex);
   BfsArgs a{dg->nindex, dg->nlist, dg->nodes, dg->edges, src, d_dist, (int*)qa, (int*)qb, (int*)hubs,
             ex->d_ctl, ex->timeout_ns, o.hub_degree, o.bfs_alpha, o.bfs_beta, nullptr, 0};
   void* args[] = {&a};
@@ -192,7 +192,7 @@ int igk_bfs_multi(IgExec* ex, const ig_csr* dg, const int* d_sources, int nsourc
   if ((rc = ig_scratch_get(ex->scratch, IG_SLOT_Q1, vb, &qb))) return rc;
   if ((rc = ig_scratch_get(ex->scratch, IG_SLOT_Q2, vb, &hubs))) return rc;
   if ((rc = ig_exec_reset(ex))) return rc;
-  const IgOptions& o = ig_options();
+  const IgOptions& o = ig_exec_options(ex);
   BfsArgs a{dg->nindex, dg->nlist, dg->nodes, dg->edges, 0, d_dist, (int*)qa, (int*)qb, (int*)hubs,
             ex->d_ctl, ex->timeout_ns, o.hub_degree, o.bfs_alpha, o.bfs_beta, d_sources, nsources};
   void* args[] = {&a};
@@ -208,7 +208,7 @@ int igk_bfs_launch_prealloc(IgExec* ex, const ig_csr* dg, int src, int* d_dist, 
   int rc = ig_cuda_check((int)cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, bfs_persistent, kThreads, 0),
                          "occupancy");
   if (rc) return rc;
-  const IgOptions& o = ig_options();
+  const IgOptions& o = ig_exec_options(ex);
   if (o.blocks_per_sm > 0) per_sm = std::min(per_sm, o.blocks_per_sm);
   if (per_sm < 1) return ig_fail(IG_ERR_CUDA, "persistent kernel cannot be resident (occupancy 0)");
   BfsArgs a{dg->nindex, dg->nlist, dg->nodes, dg->edges, src, d_dist, qa, qb, hubs,

@@ -144,7 +144,7 @@ int igk_cc(IgExec* ex, const ig_csr* dg, int* d_label) {
   int rc;
   if ((rc = ig_scratch_get(ex->scratch, IG_SLOT_Q2, (size_t)n * sizeof(int), &hubs))) return rc;
   if ((rc = ig_exec_reset(ex))) return rc;
-  const IgOptions& o = ig_options();
+  const IgOptions& o = ig_exec_options(ex);
   const int grid_v = std::min((n + kThreads - 1) / kThreads, ex->sms * 16);
   const int grid_w = std::max(1, std::min((n + kThreads - 1) / kThreads, ex->sms * 8));
   cc_init<<<grid_v, kThreads, 0, ex->stream>>>(dg->nindex, dg->nlist, n, d_label);

@@ -466,3 +466,65 @@ __device__ __forceinline__ void grid_expand_hubs4(const int* __restrict__ nindex
 }
 
 }  // namespace ig
+
+
+namespace ig {
+
+// Per-warp staging of worklist appends in shared memory.  A warp gathers the
+// items it appends in its own buffer and writes them to the global queue 32
+// at a time (one atomicAdd on the queue counter and one coalesced 128-byte
+// store per 32 items) instead of one atomicAdd per warp step on a counter that
+// every warp of the grid hits.  `n` is the warp-uniform number of buffered
+// items; warp_buf_flush must run before the items are needed (the grid
+// barrier that ends the phase).
+constexpr int kWarpBuf = 160;  // 32 + the most items one step adds (32 lanes x 4)
+
+template <int kMax>
+__device__ __forceinline__ void warp_buf_append(int cnt, const int (&items)[kMax], int* buf, int& n, int* q,
+                                                int* qsize, int cap, IgCtl* ctl) {
+  const int lane = lane_id();
+  int incl = cnt;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int t = __shfl_up_sync(IG_FULL, incl, o);
+    if (lane >= o) incl += t;
+  }
+  const int total = __shfl_sync(IG_FULL, incl, 31);
+  if (total == 0) return;
+  const int pos = n + incl - cnt;
+#pragma unroll
+  for (int k = 0; k < kMax; k++)
+    if (k < cnt) buf[pos + k] = items[k];
+  n += total;
+  __syncwarp();
+  while (n >= 32) {
+    int base = 0;
+    if (lane == 0) base = atomicAdd(qsize, 32);
+    base = __shfl_sync(IG_FULL, base, 0);
+    const int v = buf[lane];
+    if (base + lane < cap) q[base + lane] = v;
+    else raise(ctl, IG_ERR_OVERFLOW);
+    __syncwarp();
+    // move the rest down by 32: lane l reads index i and writes i - 32, and
+    // index i - 32 was read by the same lane one pass earlier
+    for (int i = 32 + lane; i < n; i += 32) buf[i - 32] = buf[i];
+    __syncwarp();
+    n -= 32;
+  }
+}
+
+__device__ __forceinline__ void warp_buf_flush(int* buf, int& n, int* q, int* qsize, int cap, IgCtl* ctl) {
+  if (n == 0) return;  // warp-uniform
+  const int lane = lane_id();
+  int base = 0;
+  if (lane == 0) base = atomicAdd(qsize, n);
+  base = __shfl_sync(IG_FULL, base, 0);
+  if (lane < n) {
+    if (base + lane < cap) q[base + lane] = buf[lane];
+    else raise(ctl, IG_ERR_OVERFLOW);
+  }
+  __syncwarp();
+  n = 0;
+}
+
+}  // namespace ig

@@ -6,6 +6,7 @@
 #include <mutex>
 
 #include "../../include/indigo_gb300.h"
+#include "ig_options.h"
 
 #ifdef __CUDACC__
 #include <cuda_runtime.h>
@@ -82,7 +83,13 @@ struct IgExec {
   int device = 0;
   int sms = 0;
   unsigned long long timeout_ns = 0;
+  const IgOptions* opts = nullptr;  // per-handle options (batch autotuning); null = process-wide
 };
+
+// Options a launcher uses for this execution context.
+inline const IgOptions& ig_exec_options(const IgExec* ex) { return ex->opts ? *ex->opts : ig_options(); }
+// Reads option `name` of `o` (same names as ig_get_option).
+int ig_options_get(const IgOptions& o, const char* name, long long* value);
 
 // Per-device state used by the drop-in entry points.
 struct IgDevice {

@@ -166,7 +166,7 @@ int igk_mis(IgExec* ex, const ig_csr* dg, int* d_status, unsigned int* d_prio) {
   if ((rc = ig_scratch_get(ex->scratch, IG_SLOT_Q0, vb, &wa))) return rc;
   if ((rc = ig_scratch_get(ex->scratch, IG_SLOT_Q1, vb, &wb))) return rc;
   if ((rc = ig_exec_reset(ex))) return rc;
-  const IgOptions& o = ig_options();
+  const IgOptions& o = ig_exec_options(ex);
   MisArgs a{dg->nindex, dg->nlist, dg->nodes, d_status, (int*)resume, (int*)wa, (int*)wb, ex->d_ctl, ex->timeout_ns};
   void* args[] = {&a};
   return ig_launch_coop(ex, (const void*)mis_persistent, kThreads, 0, o.blocks_per_sm, args, nullptr);

@@ -382,7 +382,7 @@ __global__ void __launch_bounds__(kThreads) pr_persistent(PrArgs a) {
 
 static int pr_launch(IgExec* ex, const ig_csr* dg, const int* d_degree, float* d_scores, float epsilon,
                      int max_iter, const int* d_graph_vptr, int graphs, int* d_iters) {
-  const IgOptions& o = ig_options();
+  const IgOptions& o = ig_exec_options(ex);
   const int n = dg->nodes;
   const int hub_degree = std::max(o.pr_hub_degree, 32);
   const int chunk = std::max(o.pr_chunk, 32);

@@ -676,13 +676,15 @@ extern "C" int ig_set_option(const char* name, long long value) {
   return ig_fail(IG_ERR_INVALID_ARG, "unknown option %s", name);
 }
 
-extern "C" int ig_get_option(const char* name, long long* value) {
+int ig_options_get(const IgOptions& o, const char* name, long long* value) {
   if (!name || !value) return ig_fail(IG_ERR_INVALID_ARG, "null argument");
   for (const auto& f : g_opt_fields) {
     if (strcmp(f.name, name) == 0) {
-      *value = f.get(ig_options());
+      *value = f.get(o);
       return IG_OK;
     }
   }
   return ig_fail(IG_ERR_INVALID_ARG, "unknown option %s", name);
 }
+
+extern "C" int ig_get_option(const char* name, long long* value) { return ig_options_get(ig_options(), name, value); }

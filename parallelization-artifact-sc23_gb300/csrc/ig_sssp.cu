@@ -60,7 +60,7 @@ struct SsspArgs {
 // ctl->u64[0..1]   weight-sample sum / count, ctl->u64[2] bucket width
 // ctl->work        relaxations that improved a distance
 
-__global__ void __launch_bounds__(kThreads) sssp_persistent(SsspArgs a) {
+__global__ void __launch_bounds__(kThreads, 4) sssp_persistent(SsspArgs a) {
   using namespace ig;
   IgCtl* ctl = a.ctl;
   const int lane = lane_id();
@@ -68,6 +68,10 @@ __global__ void __launch_bounds__(kThreads) sssp_persistent(SsspArgs a) {
   const long long gthreads = (long long)gridDim.x * blockDim.x;
   const int warp_g = (int)(gtid >> 5);
   const int nwarps = (int)(gthreads >> 5);
+  __shared__ int s_qbuf[kThreads / 32][2][kWarpBuf];  // per-warp staging of near / far appends
+  int* nbuf = s_qbuf[threadIdx.x >> 5][0];
+  int* fbuf = s_qbuf[threadIdx.x >> 5][1];
+  int nbuf_n = 0, fbuf_n = 0;
 
   for (long long v = gtid; v < a.nodes; v += gthreads) {
     a.dist[v] = (v == a.src) ? 0 : kInf;
@@ -131,29 +135,6 @@ __global__ void __launch_bounds__(kThreads) sssp_persistent(SsspArgs a) {
       const int far_mark = epoch + 1;
       const int* frontier = heavy ? a.members : cur;
       const int fcount = heavy ? nmem : cur_size;
-      auto relax = [&](bool act, int e, int du) {
-        bool to_near = false, to_far = false;
-        int v = 0;
-        if (act && du != kInf) {
-          const int w = __ldg(&a.eweight[e]);
-          const bool light = !a.heavy_split || (long long)w < delta;
-          if (light != heavy) {
-            v = __ldg(&a.nlist[e]);
-            const long long nd = (long long)du + w;
-            if (nd < (long long)a.dist[v]) {
-              const int ndi = (int)nd;
-              const int old = atomicMin(&a.dist[v], ndi);
-              if (ndi < old) {
-                improved++;
-                if (nd < T) to_near = a.stamp[v] != next_stamp && atomicExch(&a.stamp[v], next_stamp) != next_stamp;
-                else to_far = a.farflag[v] != far_mark && atomicExch(&a.farflag[v], far_mark) != far_mark;
-              }
-            }
-          }
-        }
-        warp_append(to_near, v, nxt, qsize, a.nodes, ctl);
-        warp_append(to_far, v, far, fsize, a.nodes, ctl);
-      };
       // Four edges per lane at a time: their loads, atomics and stamp checks
       // are independent, so they are issued together.
       auto relax4 = [&](const bool (&act)[4], const int (&e)[4], const int (&du)[4]) {
@@ -191,8 +172,8 @@ __global__ void __launch_bounds__(kThreads) sssp_persistent(SsspArgs a) {
             }
           }
         }
-        warp_append_n<4>(nn, nq, nxt, qsize, a.nodes, ctl);
-        warp_append_n<4>(nf, fq, far, fsize, a.nodes, ctl);
+        warp_buf_append<4>(nn, nq, nbuf, nbuf_n, nxt, qsize, a.nodes, ctl);
+        warp_buf_append<4>(nf, fq, fbuf, fbuf_n, far, fsize, a.nodes, ctl);
       };
       for (int base = warp_g * 32; base < fcount; base += nwarps * 32) {
         const int i = base + lane;
@@ -230,6 +211,8 @@ __global__ void __launch_bounds__(kThreads) sssp_persistent(SsspArgs a) {
           relax4(act, e, duj);
         });
       }
+      warp_buf_flush(nbuf, nbuf_n, nxt, qsize, a.nodes, ctl);
+      warp_buf_flush(fbuf, fbuf_n, far, fsize, a.nodes, ctl);
       if (!grid_sync(ctl, a.timeout_ns)) return;
       const int nh = ld_relaxed(nhub);
       if (nh > 0) {
@@ -239,6 +222,8 @@ __global__ void __launch_bounds__(kThreads) sssp_persistent(SsspArgs a) {
           for (int k = 0; k < 4; k++) duh[k] = act[k] ? a.dist[hv[k]] : kInf;
           relax4(act, e, duh);
         });
+        warp_buf_flush(nbuf, nbuf_n, nxt, qsize, a.nodes, ctl);
+        warp_buf_flush(fbuf, fbuf_n, far, fsize, a.nodes, ctl);
         if (!grid_sync(ctl, a.timeout_ns)) return;
       }
       if (heavy) mpass++;
@@ -328,7 +313,7 @@ int igk_sssp(IgExec* ex, const ig_csr* dg, int src, int* d_dist) {
   if ((rc = ig_scratch_get(ex->scratch, IG_SLOT_F1, vb, &members))) return rc;
   if ((rc = ig_scratch_get(ex->scratch, IG_SLOT_E0, vb, &inmember))) return rc;
   if ((rc = ig_exec_reset(ex))) return rc;
-  const IgOptions& o = ig_options();
+  const IgOptions& o = ig_exec_options(ex);
   SsspArgs a{dg->nindex, dg->nlist, dg->eweight, dg->nodes, dg->edges, src, d_dist,
              (int*)qa, (int*)qb, (int*)fa, (int*)fb, (int*)stamp, (int*)farflag, (int*)hubs,
              (int*)expanded, (int*)members, (int*)inmember, ex->d_ctl, ex->timeout_ns, o.hub_degree,

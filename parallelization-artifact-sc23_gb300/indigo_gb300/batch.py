@@ -114,6 +114,23 @@ class Batch:
     def pagerank(self, scores: DeviceBuffer, epsilon: float, max_iter: int, iters: DeviceBuffer):
         check(load().ig_batch_pagerank(self.h, scores.ptr, epsilon, max_iter, iters.ptr))
 
+    ALGOS = ("bfs", "cc", "tc", "pr")
+
+    def autotune(self, algos=("bfs", "cc", "pr"), reps: int = 2) -> dict:
+        """Times the launch variants of each algorithm on this batch and keeps
+        the fastest for later calls; returns {algo: best ms}."""
+        mask = 0
+        for a in algos:
+            mask |= 1 << self.ALGOS.index(a)
+        best = (ctypes.c_float * 4)()
+        check(load().ig_batch_autotune(self.h, mask, reps, best))
+        return {a: float(best[i]) for i, a in enumerate(self.ALGOS) if mask & (1 << i)}
+
+    def get_option(self, algo: str, name: str) -> int:
+        v = ctypes.c_longlong()
+        check(load().ig_batch_get_option(self.h, self.ALGOS.index(algo), name.encode(), ctypes.byref(v)))
+        return v.value
+
     def last_run(self) -> RunInfo:
         info = RunInfo()
         check(load().ig_batch_last_run(self.h, ctypes.byref(info)))

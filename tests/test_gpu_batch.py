@@ -110,3 +110,23 @@ def test_batch_of_tiny_and_edge_case_graphs(ig, gpu):
         assert np.array_equal(d[vptr[i]:vptr[i + 1]], e_dist)
         assert np.array_equal(l[vptr[i]:vptr[i + 1]], e_lab)
         assert int(c[i]) == e_tc
+
+
+def test_autotune_keeps_results(ig, gpu, expected):
+    """Autotuning picks launch variants only: after it, the batch's calls
+    (re-captured with the chosen options) give the same results."""
+    u, vptr = ig.gen_batch(48, vmin=64, vmax=4096, seed=13, maxw=255)
+    with ig.Batch(u, vptr) as b:
+        best = b.autotune(("bfs", "cc", "tc", "pr"), reps=1)
+        assert set(best) == {"bfs", "cc", "tc", "pr"} and all(v > 0 for v in best.values())
+        assert b.get_option("bfs", "blocks_per_sm") in (ig.get_option("blocks_per_sm"), 2, 4, 8)
+        assert b.get_option("cc", "hub_degree") in (ig.get_option("hub_degree"), 64, 256, 1024, 4096)
+        assert b.get_option("pr", "pr_hub_degree") in (ig.get_option("pr_hub_degree"), 1024, 4096)
+        outs = run_batch(ig, b)
+    for call, (dist, lab, cnt, sc, its) in enumerate(outs):
+        for i, (e_dist, e_lab, e_tc, e_sc, e_it) in enumerate(expected):
+            v0, v1 = b.vptr[i], b.vptr[i + 1]
+            assert np.array_equal(dist[v0:v1], e_dist), (call, i, "bfs")
+            assert np.array_equal(lab[v0:v1], e_lab), (call, i, "cc")
+            assert int(cnt[i]) == e_tc, (call, i, "tc")
+            assert int(its[i]) == e_it and np.array_equal(sc[v0:v1], e_sc), (call, i, "pr")
