@@ -212,6 +212,14 @@ __device__ __forceinline__ bool contains(const int* list, int len, int x) {
 
 __device__ __forceinline__ unsigned hash_slot(int w, unsigned mask) { return ((unsigned)w * 0x9E3779B1u >> 7) & mask; }
 
+// item_v[k] = middle vertex of work item k (items of v: [item_off[v], item_off[v+1])).
+__global__ void __launch_bounds__(kThreads) tc_item_owner(const int* __restrict__ item_off, int n, int* item_v) {
+  for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < n; v += gridDim.x * blockDim.x) {
+    const int b = item_off[v], e = item_off[v + 1];
+    for (int k = b; k < e; k++) item_v[k] = v;
+  }
+}
+
 // One work item = (middle vertex v, a chunk of kChunk of its in-neighbours u).
 // The warp hashes N+(v) into its shared-memory table, then walks the
 // out-lists N+(u) of the chunk's in-neighbours (load-balanced) and probes:
@@ -221,7 +229,8 @@ __device__ __forceinline__ unsigned hash_slot(int w, unsigned mask) { return ((u
 template <bool kBatched>
 __global__ void __launch_bounds__(kThreads) tc_count(const int* __restrict__ out_off, const int* __restrict__ out_list,
                                                      const int* __restrict__ nindex, const int* __restrict__ in_list,
-                                                     const int* __restrict__ item_off, int n,
+                                                     const int* __restrict__ item_off,
+                                                     const int* __restrict__ item_v, int n,
                                                      unsigned long long* count, const IgCtl* ctl,
                                                      const int* __restrict__ graph_vptr, int graphs) {
   using namespace ig;
@@ -239,14 +248,7 @@ __global__ void __launch_bounds__(kThreads) tc_count(const int* __restrict__ out
   unsigned mask = 0;
   bool hashed = false;
   for (int it = warp_g; it < items; it += nwarps) {
-    // middle vertex: largest v with item_off[v] <= it
-    int lo = 0, hi = n - 1;
-    while (lo < hi) {
-      const int mid = (lo + hi + 1) >> 1;
-      if (__ldg(&item_off[mid]) <= it) lo = mid;
-      else hi = mid - 1;
-    }
-    const int v = lo;
+    const int v = __ldg(&item_v[it]);  // middle vertex
     const int vb = __ldg(&out_off[v]);
     const int vd = __ldg(&out_off[v + 1]) - vb;
     if (v != cur_v) {
@@ -292,24 +294,30 @@ __global__ void __launch_bounds__(kThreads) tc_count(const int* __restrict__ out
         }
         ud = ue - ub;
       }
-      warp_expand(ub, ud, [&](bool act, int e, int) {
-        if (!act) return;
-        const int w = __ldg(&out_list[e]);
-        if (hashed) {
-          // most probes miss: the bit filter rejects them with one shared load
-          if (((bits[(w >> 5) & (kBitWords - 1)] >> (w & 31)) & 1u) == 0) return;
-          unsigned h = hash_slot(w, mask);
-          while (true) {
-            const int t = tab[h];
-            if (t == w) {
-              local++;
-              break;
+      // four 32-probe slots per step: their list loads are issued together
+      warp_expand4(ub, ud, [&](const bool (&act)[4], const int (&e)[4], const int (&)[4]) {
+        int w[4];
+#pragma unroll
+        for (int k = 0; k < 4; k++) w[k] = act[k] ? __ldg(&out_list[e[k]]) : -1;
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+          if (!act[k]) continue;
+          if (hashed) {
+            // most probes miss: the bit filter rejects them with one shared load
+            if (((bits[(w[k] >> 5) & (kBitWords - 1)] >> (w[k] & 31)) & 1u) == 0) continue;
+            unsigned h = hash_slot(w[k], mask);
+            while (true) {
+              const int t = tab[h];
+              if (t == w[k]) {
+                local++;
+                break;
+              }
+              if (t == -1) break;
+              h = (h + 1) & mask;
             }
-            if (t == -1) break;
-            h = (h + 1) & mask;
+          } else if (contains(out_list + vb, vd, w[k])) {
+            local++;
           }
-        } else if (contains(out_list + vb, vd, w)) {
-          local++;
         }
       });
     }
@@ -351,13 +359,17 @@ int igk_tc_batched(IgExec* ex, int nodes, int edges, const int* d_nindex, const 
 static int tc_run(IgExec* ex, int nodes, int edges, const int* d_nindex, const int* d_nlist, unsigned long long* d_count,
                   const int* d_graph_vptr, int graphs) {
   const size_t vb = ((size_t)nodes + 1) * sizeof(int);
-  void *cnt, *off, *icnt, *ioff, *list, *inl, *hubs;
+  void *cnt, *off, *icnt, *ioff, *list, *inl, *hubs, *itemv;
   int rc;
   if ((rc = ig_scratch_get(ex->scratch, IG_SLOT_V0, vb, &cnt))) return rc;
   if ((rc = ig_scratch_get(ex->scratch, IG_SLOT_V1, vb, &off))) return rc;
   if ((rc = ig_scratch_get(ex->scratch, IG_SLOT_V2, vb, &icnt))) return rc;
   if ((rc = ig_scratch_get(ex->scratch, IG_SLOT_Q0, vb, &ioff))) return rc;
   if ((rc = ig_scratch_get(ex->scratch, IG_SLOT_Q1, vb, &hubs))) return rc;
+  // items: sum over v of ceil(|N-(v)| / kChunk) <= edges / kChunk + nodes
+  if ((rc = ig_scratch_get(ex->scratch, IG_SLOT_Q2, ((size_t)edges / kChunk + (size_t)nodes + 1) * sizeof(int),
+                           &itemv)))
+    return rc;
   if ((rc = ig_scratch_get(ex->scratch, IG_SLOT_E0, std::max<size_t>(1, (size_t)edges) * sizeof(int), &list)))
     return rc;
   if ((rc = ig_scratch_get(ex->scratch, IG_SLOT_G1, std::max<size_t>(1, (size_t)edges) * sizeof(int), &inl)))
@@ -388,14 +400,16 @@ static int tc_run(IgExec* ex, int nodes, int edges, const int* d_nindex, const i
                                                      (int*)inl, ex->d_ctl);
   tc_orient_hubs_fill<<<ex->sms * 8, kThreads, 0, ex->stream>>>(d_nindex, d_nlist, (const int*)hubs,
                                                                 (const int*)off, (int*)list, (int*)inl, ex->d_ctl);
+  tc_item_owner<<<grid, kThreads, 0, ex->stream>>>((const int*)ioff, nodes, (int*)itemv);
   if (d_graph_vptr)
     tc_count<true><<<ex->sms * 3, kThreads, smem, ex->stream>>>((const int*)off, (const int*)list, d_nindex,
-                                                                (const int*)inl, (const int*)ioff, nodes, d_count,
-                                                                ex->d_ctl, d_graph_vptr, graphs);
+                                                                (const int*)inl, (const int*)ioff, (const int*)itemv,
+                                                                nodes, d_count, ex->d_ctl, d_graph_vptr, graphs);
   else
     tc_count<false><<<ex->sms * 3, kThreads, smem, ex->stream>>>((const int*)off, (const int*)list, d_nindex,
-                                                                 (const int*)inl, (const int*)ioff, nodes, d_count,
-                                                                 ex->d_ctl, nullptr, 0);
-  ig_count_launches(5);
+                                                                 (const int*)inl, (const int*)ioff,
+                                                                 (const int*)itemv, nodes, d_count, ex->d_ctl,
+                                                                 nullptr, 0);
+  ig_count_launches(6);
   return ig_cuda_check((int)cudaGetLastError(), "tc launch");
 }
