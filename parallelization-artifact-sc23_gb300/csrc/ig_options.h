@@ -9,6 +9,7 @@ struct IgOptions {
   long long sssp_delta;   // near/far bucket width (0 = derived from sampled weights)
   int sssp_delta_scale;   // derived width = mean weight * scale / mean degree
   int sssp_heavy_split;   // 1: heavy edges (w >= delta) relaxed once per bucket
+  int sssp_hub_degree;    // SSSP: degree above which a vertex is expanded by the whole grid
   int pr_hub_degree;      // PageRank: degree above which a vertex is split in chunks
   int pr_chunk;           // PageRank: edges per hub chunk
 };

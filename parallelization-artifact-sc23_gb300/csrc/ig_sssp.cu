@@ -216,12 +216,11 @@ __global__ void __launch_bounds__(kThreads, 4) sssp_persistent(SsspArgs a) {
       if (!grid_sync(ctl, a.timeout_ns)) return;
       const int nh = ld_relaxed(nhub);
       if (nh > 0) {
-        grid_expand_hubs4(a.nindex, a.hubs, nh, [&](const bool (&act)[4], const int (&e)[4], const int (&hv)[4]) {
-          int duh[4];
-#pragma unroll
-          for (int k = 0; k < 4; k++) duh[k] = act[k] ? a.dist[hv[k]] : kInf;
-          relax4(act, e, duh);
-        });
+        // hub distances are read once per staged hub; a hub improved since
+        // was queued again and is expanded with its new distance next round
+        grid_expand_hubs4(
+            a.nindex, a.hubs, nh, [&](int v) { return a.dist[v]; },
+            [&](const bool (&act)[4], const int (&e)[4], const int (&)[4], const int (&du)[4]) { relax4(act, e, du); });
         warp_buf_flush(nbuf, nbuf_n, nxt, qsize, a.nodes, ctl);
         warp_buf_flush(fbuf, fbuf_n, far, fsize, a.nodes, ctl);
         if (!grid_sync(ctl, a.timeout_ns)) return;
@@ -316,7 +315,7 @@ int igk_sssp(IgExec* ex, const ig_csr* dg, int src, int* d_dist) {
   const IgOptions& o = ig_exec_options(ex);
   SsspArgs a{dg->nindex, dg->nlist, dg->eweight, dg->nodes, dg->edges, src, d_dist,
              (int*)qa, (int*)qb, (int*)fa, (int*)fb, (int*)stamp, (int*)farflag, (int*)hubs,
-             (int*)expanded, (int*)members, (int*)inmember, ex->d_ctl, ex->timeout_ns, o.hub_degree,
+             (int*)expanded, (int*)members, (int*)inmember, ex->d_ctl, ex->timeout_ns, o.sssp_hub_degree,
              o.sssp_delta, o.sssp_delta_scale, o.sssp_heavy_split};
   void* args[] = {&a};
   return ig_launch_coop(ex, (const void*)sssp_persistent, kThreads, 0, o.blocks_per_sm, args, nullptr);
