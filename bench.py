@@ -45,7 +45,6 @@ RUNS_PER_STEP = 2 * N_SOURCES + 4
 METRIC = "GTEPS (RMAT-22: 16x BFS + 16x SSSP + CC + MIS + PR + TC)"
 UNIT = "GTEPS"
 ALGOS = ["bfs", "sssp", "cc", "mis", "pr", "tc"]
-LAUNCHES_PER_CALL = {"bfs": 1, "sssp": 1, "cc": 4, "mis": 1, "pr": 1, "tc": 3}  # dominant-kernel launches
 
 
 def log(*a):

@@ -28,16 +28,28 @@ namespace {
 
 constexpr int kThreads = 256;
 constexpr int kWarps = kThreads / 32;
-constexpr int kChunk = 64;      // in-neighbours per work item
-constexpr int kOrientHub = 256; // lists longer than this are split by one block each
-constexpr int kHashCap = 2048;  // hash slots per warp (out-degree <= 1024 is hashed)
-constexpr int kBitWords = 256;  // 8192-bit filter per warp: bit (w mod 8192) set for w in N+(v)
+constexpr int kOrientHub = 256;   // lists longer than this are split by one block each
+constexpr int kBlockOut = 64;     // middle vertices with more out-neighbours are counted by whole blocks
+constexpr int kChunk = 64;        // in-neighbours per warp work item
+constexpr int kBlockChunk = 1024; // in-neighbours per block work item
+constexpr int kHashCap = 2048;    // block table slots (out-degree <= 1024 is hashed)
+constexpr int kBitWords = 256;    // block filter: 8192 bits, bit (w mod 8192) set for w in N+(v)
+constexpr int kWarpCap = 128;     // warp table slots (out-degree <= kBlockOut)
+constexpr int kWarpBitWords = 64; // warp filter: 2048 bits
+
+// Work items of middle vertex v with `out` out-neighbours and `in`
+// in-neighbours: warp items of kChunk in-neighbours for a short N+(v), block
+// items of kBlockChunk for a long one (the block shares one table of N+(v)).
+__device__ __forceinline__ void tc_items(int out, int in, int* warp_items, int* block_items) {
+  *warp_items = (out > 0 && out <= kBlockOut) ? (in + kChunk - 1) / kChunk : 0;
+  *block_items = out > kBlockOut ? (in + kBlockChunk - 1) / kBlockChunk : 0;
+}
 
 __device__ __forceinline__ bool before(int du, int u, int dw, int w) { return du < dw || (du == dw && u < w); }
 
 __global__ void __launch_bounds__(kThreads) tc_orient_count(const int* __restrict__ nindex,
                                                             const int* __restrict__ nlist, int n, int* out_cnt,
-                                                            int* item_cnt, int* hubs, IgCtl* ctl) {
+                                                            int* item_cnt, int* item_cnt_b, int* hubs, IgCtl* ctl) {
   using namespace ig;
   __shared__ int s_cnt[kWarps][32];
   const int lane = lane_id(), wib = threadIdx.x >> 5;
@@ -76,8 +88,7 @@ __global__ void __launch_bounds__(kThreads) tc_orient_count(const int* __restric
     if (v < n && !hub) {
       const int oc = s_cnt[wib][lane];
       out_cnt[v] = oc;
-      // work items of middle vertex v: its in-neighbours in chunks of kChunk
-      item_cnt[v] = oc > 0 ? (deg - oc + kChunk - 1) / kChunk : 0;
+      tc_items(oc, deg - oc, &item_cnt[v], &item_cnt_b[v]);
     }
     __syncwarp();
   }
@@ -141,7 +152,7 @@ __global__ void __launch_bounds__(kThreads) tc_orient_fill(const int* __restrict
 __global__ void __launch_bounds__(kThreads) tc_orient_hubs_count(const int* __restrict__ nindex,
                                                                  const int* __restrict__ nlist, int n,
                                                                  const int* hubs, int* out_cnt, int* item_cnt,
-                                                                 IgCtl* ctl) {
+                                                                 int* item_cnt_b, IgCtl* ctl) {
   using namespace ig;
   __shared__ int s_tmp[33];
   const int nh = ctl->i32[0];
@@ -160,7 +171,7 @@ __global__ void __launch_bounds__(kThreads) tc_orient_hubs_count(const int* __re
     block_scan_int(keep, s_tmp, &total);
     if (threadIdx.x == 0) {
       out_cnt[u] = total;
-      item_cnt[u] = total > 0 ? (du - total + kChunk - 1) / kChunk : 0;
+      tc_items(total, du - total, &item_cnt[u], &item_cnt_b[u]);
     }
     __syncthreads();
   }
@@ -220,29 +231,109 @@ __global__ void __launch_bounds__(kThreads) tc_item_owner(const int* __restrict_
   }
 }
 
-// One work item = (middle vertex v, a chunk of kChunk of its in-neighbours u).
-// The warp hashes N+(v) into its shared-memory table, then walks the
-// out-lists N+(u) of the chunk's in-neighbours (load-balanced) and probes:
-// w in N+(u) and in N+(v) closes the triangle u -> v -> w, counted once at v.
+// Probes of one group of <= 32 in-neighbours u of middle vertex v, one per
+// lane (in_list[g .. gend)): every w of N+(u) (only the part after v when ids
+// are in (degree, id) order) is looked up in N+(v): filter bit first, then the
+// hash table (or a binary search of N+(v) when it was too long to hash).  A
+// hit closes the triangle u -> v -> w, counted once at v.  Returns this lane's
+// hits.  All lanes of the warp call it.
+template <int kBits>
+__device__ __forceinline__ unsigned long long probe_group(const int* __restrict__ out_off,
+                                                          const int* __restrict__ out_list,
+                                                          const int* __restrict__ in_list, int g, int gend, int v,
+                                                          int vb, int vd, bool ranked, const int* tab,
+                                                          const unsigned* bits, unsigned mask, bool hashed) {
+  using namespace ig;
+  const int lane = lane_id();
+  unsigned long long local = 0;
+  int ub = 0, ud = 0;
+  if (g + lane < gend) {
+    const int u = __ldg(&in_list[g + lane]);
+    ub = __ldg(&out_off[u]);
+    const int ue = __ldg(&out_off[u + 1]);
+    if (ranked) {
+      // rank order = id order: only w > v in N+(u) can close u -> v -> w
+      int lo2 = ub, hi2 = ue;
+      while (lo2 < hi2) {
+        const int mid = (lo2 + hi2) >> 1;
+        if (__ldg(&out_list[mid]) <= v) lo2 = mid + 1;
+        else hi2 = mid;
+      }
+      ub = lo2;
+    }
+    ud = ue - ub;
+  }
+  // four 32-probe slots per step: their list loads are issued together
+  warp_expand4(ub, ud, [&](const bool (&act)[4], const int (&e)[4], const int (&)[4]) {
+    int w[4];
+#pragma unroll
+    for (int k = 0; k < 4; k++) w[k] = act[k] ? __ldg(&out_list[e[k]]) : -1;
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+      if (!act[k]) continue;
+      if (hashed) {
+        // most probes miss: the filter rejects them with one shared load
+        if (((bits[(w[k] >> 5) & (kBits - 1)] >> (w[k] & 31)) & 1u) == 0) continue;
+        unsigned h = hash_slot(w[k], mask);
+        while (true) {
+          const int t = tab[h];
+          if (t == w[k]) {
+            local++;
+            break;
+          }
+          if (t == -1) break;
+          h = (h + 1) & mask;
+        }
+      } else if (contains(out_list + vb, vd, w[k])) {
+        local++;
+      }
+    }
+  });
+  return local;
+}
+
+// graph of vertex v in a batch: largest g with graph_vptr[g] <= v
+__device__ __forceinline__ int tc_graph_of(const int* __restrict__ graph_vptr, int graphs, int v) {
+  int lo = 0, hi = graphs - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (__ldg(&graph_vptr[mid]) <= v) lo = mid;
+    else hi = mid - 1;
+  }
+  return lo;
+}
+
+// Adds the warp's hits since `before` to the count of v's graph (batched form).
+__device__ __forceinline__ void tc_add_graph(unsigned long long mine, unsigned long long* count,
+                                             const int* graph_vptr, int graphs, int v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) mine += __shfl_xor_sync(IG_FULL, mine, o);
+  if (ig::lane_id() == 0 && mine) atomicAdd(&count[tc_graph_of(graph_vptr, graphs, v)], mine);
+}
+
+// Warp work items: (middle vertex v with out-degree <= kBlockOut, kChunk of
+// its in-neighbours).  The warp hashes N+(v) into its own small table.
 // kBatched: the graph is a disjoint union; triangles are added to the count of
 // the graph that holds their middle vertex (graph_vptr: first vertex of each graph).
 template <bool kBatched>
-__global__ void __launch_bounds__(kThreads) tc_count(const int* __restrict__ out_off, const int* __restrict__ out_list,
-                                                     const int* __restrict__ nindex, const int* __restrict__ in_list,
-                                                     const int* __restrict__ item_off,
-                                                     const int* __restrict__ item_v, int n,
-                                                     unsigned long long* count, const IgCtl* ctl,
-                                                     const int* __restrict__ graph_vptr, int graphs) {
+__global__ void __launch_bounds__(kThreads) tc_count_warp(const int* __restrict__ out_off,
+                                                          const int* __restrict__ out_list,
+                                                          const int* __restrict__ nindex,
+                                                          const int* __restrict__ in_list,
+                                                          const int* __restrict__ item_off,
+                                                          const int* __restrict__ item_v, int n,
+                                                          unsigned long long* count, const IgCtl* ctl,
+                                                          const int* __restrict__ graph_vptr, int graphs) {
   using namespace ig;
-  extern __shared__ int s_tab[];
+  __shared__ int s_tab[kWarps][kWarpCap + kWarpBitWords];
   if (ctl->err) return;
   const int lane = lane_id(), wib = threadIdx.x >> 5;
-  int* tab = s_tab + wib * (kHashCap + kBitWords);
-  unsigned* bits = (unsigned*)(tab + kHashCap);
+  int* tab = s_tab[wib];
+  unsigned* bits = (unsigned*)(tab + kWarpCap);
   const int warp_g = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int nwarps = (gridDim.x * blockDim.x) >> 5;
   const int items = __ldg(&item_off[n]);
-  const bool ids_ranked = ctl->i32[1] == 0;
+  const bool ranked = ctl->i32[1] == 0;
   unsigned long long local = 0;
   int cur_v = -1;
   unsigned mask = 0;
@@ -253,18 +344,18 @@ __global__ void __launch_bounds__(kThreads) tc_count(const int* __restrict__ out
     const int vd = __ldg(&out_off[v + 1]) - vb;
     if (v != cur_v) {
       cur_v = v;
-      hashed = 2 * vd <= kHashCap;
+      hashed = 2 * vd <= kWarpCap;
       if (hashed) {
         int cap = 32;
         while (cap < 2 * vd) cap <<= 1;
         mask = (unsigned)cap - 1;
         __syncwarp();
         for (int k = lane; k < cap; k += 32) tab[k] = -1;
-        for (int k = lane; k < kBitWords; k += 32) bits[k] = 0u;
+        for (int k = lane; k < kWarpBitWords; k += 32) bits[k] = 0u;
         __syncwarp();
         for (int k = lane; k < vd; k += 32) {
           const int w = __ldg(&out_list[vb + k]);
-          atomicOr(&bits[(w >> 5) & (kBitWords - 1)], 1u << (w & 31));
+          atomicOr(&bits[(w >> 5) & (kWarpBitWords - 1)], 1u << (w & 31));
           unsigned h = hash_slot(w, mask);
           while (atomicCAS(&tab[h], -1, w) != -1) h = (h + 1) & mask;
         }
@@ -276,70 +367,88 @@ __global__ void __launch_bounds__(kThreads) tc_count(const int* __restrict__ out
     const int c0 = ib + (it - __ldg(&item_off[v])) * kChunk;
     const int c1 = min(c0 + kChunk, iend);
     const unsigned long long before_item = local;
-    for (int g = c0; g < c1; g += 32) {
-      int ub = 0, ud = 0;
-      if (g + lane < c1) {
-        const int u = __ldg(&in_list[g + lane]);
-        ub = __ldg(&out_off[u]);
-        const int ue = __ldg(&out_off[u + 1]);
-        if (ids_ranked) {
-          // rank order = id order: only w > v in N+(u) can close u -> v -> w
-          int lo2 = ub, hi2 = ue;
-          while (lo2 < hi2) {
-            const int mid = (lo2 + hi2) >> 1;
-            if (__ldg(&out_list[mid]) <= v) lo2 = mid + 1;
-            else hi2 = mid;
-          }
-          ub = lo2;
-        }
-        ud = ue - ub;
-      }
-      // four 32-probe slots per step: their list loads are issued together
-      warp_expand4(ub, ud, [&](const bool (&act)[4], const int (&e)[4], const int (&)[4]) {
-        int w[4];
-#pragma unroll
-        for (int k = 0; k < 4; k++) w[k] = act[k] ? __ldg(&out_list[e[k]]) : -1;
-#pragma unroll
-        for (int k = 0; k < 4; k++) {
-          if (!act[k]) continue;
-          if (hashed) {
-            // most probes miss: the bit filter rejects them with one shared load
-            if (((bits[(w[k] >> 5) & (kBitWords - 1)] >> (w[k] & 31)) & 1u) == 0) continue;
-            unsigned h = hash_slot(w[k], mask);
-            while (true) {
-              const int t = tab[h];
-              if (t == w[k]) {
-                local++;
-                break;
-              }
-              if (t == -1) break;
-              h = (h + 1) & mask;
-            }
-          } else if (contains(out_list + vb, vd, w[k])) {
-            local++;
-          }
-        }
-      });
-    }
-    if (kBatched) {
-      unsigned long long mine = local - before_item;
-#pragma unroll
-      for (int o = 16; o > 0; o >>= 1) mine += __shfl_xor_sync(IG_FULL, mine, o);
-      if (lane == 0 && mine) {
-        int glo = 0, ghi = graphs - 1;  // graph of v: largest g with graph_vptr[g] <= v
-        while (glo < ghi) {
-          const int mid = (glo + ghi + 1) >> 1;
-          if (__ldg(&graph_vptr[mid]) <= v) glo = mid;
-          else ghi = mid - 1;
-        }
-        atomicAdd(&count[glo], mine);
-      }
-    }
+    for (int g = c0; g < c1; g += 32)
+      local += probe_group<kWarpBitWords>(out_off, out_list, in_list, g, c1, v, vb, vd, ranked, tab, bits, mask,
+                                          hashed);
+    if (kBatched) tc_add_graph(local - before_item, count, graph_vptr, graphs, v);
   }
-  if (kBatched) return;
+  if constexpr (!kBatched) {
 #pragma unroll
-  for (int o = 16; o > 0; o >>= 1) local += __shfl_xor_sync(IG_FULL, local, o);
-  if (lane == 0 && local) atomicAdd(count, local);
+    for (int o = 16; o > 0; o >>= 1) local += __shfl_xor_sync(IG_FULL, local, o);
+    if (lane == 0 && local) atomicAdd(count, local);
+  }
+}
+// Block work items: (middle vertex v with out-degree > kBlockOut, up to
+// kBlockChunk of its in-neighbours).  The block hashes N+(v) once into one
+// shared table (9 KB instead of a 9 KB table per warp, so eight blocks fit
+// on an SM) and its warps take groups of 32 in-neighbours from a shared
+// counter until the item is done.
+template <bool kBatched>
+__global__ void __launch_bounds__(kThreads, 8) tc_count_block(const int* __restrict__ out_off,
+                                                              const int* __restrict__ out_list,
+                                                              const int* __restrict__ nindex,
+                                                              const int* __restrict__ in_list,
+                                                              const int* __restrict__ item_off,
+                                                              const int* __restrict__ item_v, int n,
+                                                              unsigned long long* count, const IgCtl* ctl,
+                                                              const int* __restrict__ graph_vptr, int graphs) {
+  using namespace ig;
+  __shared__ int tab[kHashCap];
+  __shared__ unsigned bits[kBitWords];
+  __shared__ int s_next;
+  if (ctl->err) return;
+  const int lane = lane_id();
+  const int items = __ldg(&item_off[n]);
+  const bool ranked = ctl->i32[1] == 0;
+  unsigned long long local = 0;
+  int cur_v = -1;
+  unsigned mask = 0;
+  bool hashed = false;
+  for (int it = blockIdx.x; it < items; it += gridDim.x) {
+    const int v = __ldg(&item_v[it]);  // middle vertex (block-uniform)
+    const int vb = __ldg(&out_off[v]);
+    const int vd = __ldg(&out_off[v + 1]) - vb;
+    __syncthreads();  // the previous item's probes are done with the table and the counter
+    if (v != cur_v) {
+      cur_v = v;
+      hashed = 2 * vd <= kHashCap;
+      if (hashed) {
+        int cap = 32;
+        while (cap < 2 * vd) cap <<= 1;
+        mask = (unsigned)cap - 1;
+        for (int k = threadIdx.x; k < cap; k += blockDim.x) tab[k] = -1;
+        for (int k = threadIdx.x; k < kBitWords; k += blockDim.x) bits[k] = 0u;
+        __syncthreads();
+        for (int k = threadIdx.x; k < vd; k += blockDim.x) {
+          const int w = __ldg(&out_list[vb + k]);
+          atomicOr(&bits[(w >> 5) & (kBitWords - 1)], 1u << (w & 31));
+          unsigned h = hash_slot(w, mask);
+          while (atomicCAS(&tab[h], -1, w) != -1) h = (h + 1) & mask;
+        }
+      }
+    }
+    if (threadIdx.x == 0) s_next = 0;
+    __syncthreads();
+    const int ib = __ldg(&nindex[v]) - vb;  // in_off[v]
+    const int iend = __ldg(&nindex[v + 1]) - __ldg(&out_off[v + 1]);
+    const int c0 = ib + (it - __ldg(&item_off[v])) * kBlockChunk;
+    const int c1 = min(c0 + kBlockChunk, iend);
+    const unsigned long long before_item = local;
+    while (true) {
+      int g = 0;
+      if (lane == 0) g = atomicAdd(&s_next, 32);
+      g = c0 + __shfl_sync(IG_FULL, g, 0);
+      if (g >= c1) break;
+      local += probe_group<kBitWords>(out_off, out_list, in_list, g, c1, v, vb, vd, ranked, tab, bits, mask,
+                                      hashed);
+    }
+    if (kBatched) tc_add_graph(local - before_item, count, graph_vptr, graphs, v);
+  }
+  if constexpr (!kBatched) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) local += __shfl_xor_sync(IG_FULL, local, o);
+    if (lane == 0 && local) atomicAdd(count, local);
+  }
 }
 
 }  // namespace
@@ -359,16 +468,21 @@ int igk_tc_batched(IgExec* ex, int nodes, int edges, const int* d_nindex, const 
 static int tc_run(IgExec* ex, int nodes, int edges, const int* d_nindex, const int* d_nlist, unsigned long long* d_count,
                   const int* d_graph_vptr, int graphs) {
   const size_t vb = ((size_t)nodes + 1) * sizeof(int);
-  void *cnt, *off, *icnt, *ioff, *list, *inl, *hubs, *itemv;
+  void *cnt, *off, *icnt, *ioff, *icnt_b, *ioff_b, *list, *inl, *hubs, *itemv, *itemv_b;
   int rc;
   if ((rc = ig_scratch_get(ex->scratch, IG_SLOT_V0, vb, &cnt))) return rc;
   if ((rc = ig_scratch_get(ex->scratch, IG_SLOT_V1, vb, &off))) return rc;
   if ((rc = ig_scratch_get(ex->scratch, IG_SLOT_V2, vb, &icnt))) return rc;
   if ((rc = ig_scratch_get(ex->scratch, IG_SLOT_Q0, vb, &ioff))) return rc;
+  if ((rc = ig_scratch_get(ex->scratch, IG_SLOT_F0, vb, &icnt_b))) return rc;
+  if ((rc = ig_scratch_get(ex->scratch, IG_SLOT_F1, vb, &ioff_b))) return rc;
   if ((rc = ig_scratch_get(ex->scratch, IG_SLOT_Q1, vb, &hubs))) return rc;
-  // items: sum over v of ceil(|N-(v)| / kChunk) <= edges / kChunk + nodes
+  // items: sum over v of ceil(|N-(v)| / chunk) <= edges / chunk + nodes
   if ((rc = ig_scratch_get(ex->scratch, IG_SLOT_Q2, ((size_t)edges / kChunk + (size_t)nodes + 1) * sizeof(int),
                            &itemv)))
+    return rc;
+  if ((rc = ig_scratch_get(ex->scratch, IG_SLOT_Q3,
+                           ((size_t)edges / kBlockChunk + (size_t)nodes + 1) * sizeof(int), &itemv_b)))
     return rc;
   if ((rc = ig_scratch_get(ex->scratch, IG_SLOT_E0, std::max<size_t>(1, (size_t)edges) * sizeof(int), &list)))
     return rc;
@@ -379,37 +493,38 @@ static int tc_run(IgExec* ex, int nodes, int edges, const int* d_nindex, const i
   if ((rc = ig_cuda_check((int)cudaMemsetAsync(d_count, 0, ncount * sizeof(unsigned long long), ex->stream),
                           "memset")))
     return rc;
-  static bool attr_set[2][64] = {};
-  const size_t smem = (size_t)kWarps * (kHashCap + kBitWords) * sizeof(int);
-  const int bi = d_graph_vptr ? 1 : 0;
-  if (ex->device >= 0 && ex->device < 64 && !attr_set[bi][ex->device]) {
-    const void* fn = d_graph_vptr ? (const void*)tc_count<true> : (const void*)tc_count<false>;
-    if ((rc = ig_cuda_check((int)cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
-                            "tc smem attribute")))
-      return rc;
-    attr_set[bi][ex->device] = true;
-  }
   const int grid = std::max(1, std::min((nodes + kThreads - 1) / kThreads, ex->sms * 8));
-  tc_orient_count<<<grid, kThreads, 0, ex->stream>>>(d_nindex, d_nlist, nodes, (int*)cnt, (int*)icnt, (int*)hubs,
-                                                      ex->d_ctl);
+  tc_orient_count<<<grid, kThreads, 0, ex->stream>>>(d_nindex, d_nlist, nodes, (int*)cnt, (int*)icnt, (int*)icnt_b,
+                                                      (int*)hubs, ex->d_ctl);
   tc_orient_hubs_count<<<ex->sms * 8, kThreads, 0, ex->stream>>>(d_nindex, d_nlist, nodes, (const int*)hubs,
-                                                                 (int*)cnt, (int*)icnt, ex->d_ctl);
+                                                                 (int*)cnt, (int*)icnt, (int*)icnt_b, ex->d_ctl);
   if ((rc = igk_exclusive_scan(ex, (const int*)cnt, (int*)off, nodes, nullptr))) return rc;
   if ((rc = igk_exclusive_scan(ex, (const int*)icnt, (int*)ioff, nodes, nullptr))) return rc;
+  if ((rc = igk_exclusive_scan(ex, (const int*)icnt_b, (int*)ioff_b, nodes, nullptr))) return rc;
   tc_orient_fill<<<grid, kThreads, 0, ex->stream>>>(d_nindex, d_nlist, nodes, (const int*)off, (int*)list,
                                                      (int*)inl, ex->d_ctl);
   tc_orient_hubs_fill<<<ex->sms * 8, kThreads, 0, ex->stream>>>(d_nindex, d_nlist, (const int*)hubs,
                                                                 (const int*)off, (int*)list, (int*)inl, ex->d_ctl);
   tc_item_owner<<<grid, kThreads, 0, ex->stream>>>((const int*)ioff, nodes, (int*)itemv);
-  if (d_graph_vptr)
-    tc_count<true><<<ex->sms * 3, kThreads, smem, ex->stream>>>((const int*)off, (const int*)list, d_nindex,
-                                                                (const int*)inl, (const int*)ioff, (const int*)itemv,
-                                                                nodes, d_count, ex->d_ctl, d_graph_vptr, graphs);
-  else
-    tc_count<false><<<ex->sms * 3, kThreads, smem, ex->stream>>>((const int*)off, (const int*)list, d_nindex,
-                                                                 (const int*)inl, (const int*)ioff,
-                                                                 (const int*)itemv, nodes, d_count, ex->d_ctl,
-                                                                 nullptr, 0);
-  ig_count_launches(6);
+  tc_item_owner<<<grid, kThreads, 0, ex->stream>>>((const int*)ioff_b, nodes, (int*)itemv_b);
+  const int cgrid = ex->sms * 8;
+  if (d_graph_vptr) {
+    tc_count_block<true><<<cgrid, kThreads, 0, ex->stream>>>((const int*)off, (const int*)list, d_nindex,
+                                                             (const int*)inl, (const int*)ioff_b,
+                                                             (const int*)itemv_b, nodes, d_count, ex->d_ctl,
+                                                             d_graph_vptr, graphs);
+    tc_count_warp<true><<<cgrid, kThreads, 0, ex->stream>>>((const int*)off, (const int*)list, d_nindex,
+                                                            (const int*)inl, (const int*)ioff, (const int*)itemv,
+                                                            nodes, d_count, ex->d_ctl, d_graph_vptr, graphs);
+  } else {
+    tc_count_block<false><<<cgrid, kThreads, 0, ex->stream>>>((const int*)off, (const int*)list, d_nindex,
+                                                              (const int*)inl, (const int*)ioff_b,
+                                                              (const int*)itemv_b, nodes, d_count, ex->d_ctl,
+                                                              nullptr, 0);
+    tc_count_warp<false><<<cgrid, kThreads, 0, ex->stream>>>((const int*)off, (const int*)list, d_nindex,
+                                                             (const int*)inl, (const int*)ioff, (const int*)itemv,
+                                                             nodes, d_count, ex->d_ctl, nullptr, 0);
+  }
+  ig_count_launches(8);
   return ig_cuda_check((int)cudaGetLastError(), "tc launch");
 }
