@@ -12,15 +12,18 @@
 //   2. orient : edge u->w iff (deg u, u) < (deg w, w), so every vertex keeps
 //               O(sqrt E) out-neighbours N+; each list is split into its out
 //               part (id order) and its in part N-; counted, scanned, filled
-//   3. count  : work item = (middle vertex v, <= kChunk in-neighbours u of
-//               v).  The warp hashes N+(v) into shared memory and probes
-//               every w of the out-lists N+(u) (load-balanced warp
-//               expansion); a hit is the triangle u -> v -> w, counted once
-//               (at its middle vertex).  Work: sum over u of |N+(u)|^2 probes,
+//   3. count  : work item = (middle vertex v, a chunk of its in-neighbours
+//               u).  N+(v) is hashed into shared memory (a 2048-slot table
+//               and an 8192-bit filter shared by a whole block when N+(v)
+//               has more than 64 entries, a 128-slot table per warp
+//               otherwise) and every w of the out-lists N+(u) is probed
+//               (load-balanced warp expansion, four probes per lane in
+//               flight); a hit is the triangle u -> v -> w, counted once (at
+//               its middle vertex).  Work: sum over u of |N+(u)|^2 probes,
 //               halved when the ids are already in (degree, id) order (the
-//               degree-ordered input of the benchmark): then only the part of
-//               N+(u) after v is scanned.  A shared-memory bit filter rejects
-//               most misses before the hash probe.
+//               degree-ordered input of the benchmark): then only the part
+//               of N+(u) after v is scanned.  The filter rejects most misses
+//               before the hash probe.
 #include "ig_device.cuh"
 #include "ig_options.h"
 
