@@ -9,10 +9,10 @@
 //         the new bits into `visited`, counts them per lane, adds their
 //         distance to the lane's sum and records target hits.  A lane's BFS
 //         levels count from the step it was admitted in.
-//   SSSP: per vertex 64 int32 distances (lane-contiguous, so one edge reads and
-//         relaxes all lanes with coalesced accesses) and a 64-bit changed
-//         mask.  One round relaxes the out-edges of every vertex with changed
-//         lanes, for those lanes only (Bellman-Ford rounds).
+//   SSSP: per vertex 64 int32 distances (lane-contiguous rows) and a 64-bit
+//         changed mask.  One round relaxes the out-edges of every vertex with
+//         changed lanes, for those lanes only (Bellman-Ford rounds); a warp
+//         step takes 32 independent (edge, changed lane) pairs.
 // A lane retires when a step adds nothing for it; its results are read, its
 // state cleared, and the lane admits the next pending query at the following
 // step boundary, while the other lanes keep going (continuous batching).
@@ -197,14 +197,40 @@ struct SsspLaneState {
   unsigned long long reached[kLanes];
   unsigned long long sum[kLanes];
   long long maxd[kLanes];
-  unsigned long long cnt[kLanes];  // relaxations that improved the lane in the last round
+  unsigned long long cnt[kLanes];  // non-zero if the lane improved a distance in the last round
 };
 
+// Position of the r-th set bit (r counted from 0) of a 64-bit mask.
+__device__ __forceinline__ int nth_set_bit(u64 m, int r) {
+  unsigned x = (unsigned)m;
+  int pos = 0;
+  const int c0 = __popc(x);
+  if (r >= c0) {
+    r -= c0;
+    x = (unsigned)(m >> 32);
+    pos = 32;
+  }
+#pragma unroll
+  for (int width = 16; width >= 1; width >>= 1) {
+    const int c = __popc(x & ((1u << width) - 1u));
+    if (r >= c) {
+      r -= c;
+      x >>= width;
+      pos += width;
+    }
+  }
+  return pos;
+}
+
 // One round: for every vertex u with changed lanes, relax its out-edges for
-// those lanes.  A warp takes one edge at a time; lane q handles sources q and
-// q + 32 (the distance rows are lane-contiguous).  Frontier vertices are dealt
-// to warps in edge-balanced chunks: a warp owns `kChunk` consecutive edges of
-// the concatenated frontier lists (prefix in eoff).
+// those lanes.  The work is the (edge, changed lane) pairs: a vertex with k
+// changed lanes gives each warp step 32 / k of its edges, so a vertex that
+// changed in one or two lanes does not leave the warp idle, and the 32 pairs
+// of a step are independent (their loads and atomics overlap).  Frontier
+// vertices are dealt to warps in edge-balanced chunks: a warp owns
+// `kEdgeChunk` consecutive edges of the concatenated frontier lists (prefix in
+// eoff).  A vertex first changed in this round is appended to tlist through
+// the warp's shared-memory buffer.
 constexpr int kEdgeChunk = 64;
 
 __global__ void __launch_bounds__(kThreads) msssp_round(const int* __restrict__ nindex, const int* __restrict__ nlist,
@@ -213,24 +239,14 @@ __global__ void __launch_bounds__(kThreads) msssp_round(const int* __restrict__ 
                                                         u64* changed_next, int* dist, int* tlist, int* tsize,
                                                         SsspLaneState* st, IgCtl* ctl) {
   using namespace ig;
+  __shared__ int s_buf[kThreads / 32][kWarpBuf];
+  int* buf = s_buf[threadIdx.x >> 5];
+  int nbuf = 0;
   const int lane = lane_id();
   const int warp_g = (int)(((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5);
   const int nwarps = (int)(((long long)gridDim.x * blockDim.x) >> 5);
   const long long total = eoff[fsize];
-  unsigned long long improved[2] = {0, 0};
-  int pending = 0;   // vertices to append, one per lane slot
-  int my_push = 0;
-  auto flush = [&]() {
-    if (pending == 0) return;
-    int base = 0;
-    if (lane == 0) base = atomicAdd(tsize, pending);
-    base = __shfl_sync(IG_FULL, base, 0);
-    if (lane < pending) {
-      if (base + lane < n) tlist[base + lane] = my_push;
-      else raise(ctl, IG_ERR_OVERFLOW);
-    }
-    pending = 0;
-  };
+  u64 imp_lanes = 0;  // source lanes this thread improved
   for (long long c0 = (long long)warp_g * kEdgeChunk; c0 < total; c0 += (long long)nwarps * kEdgeChunk) {
     const long long c1 = min(c0 + kEdgeChunk, total);
     // owner of c0: largest i with eoff[i] <= c0
@@ -241,52 +257,48 @@ __global__ void __launch_bounds__(kThreads) msssp_round(const int* __restrict__ 
       else hi = mid - 1;
     }
     int fi = lo;
-    int u = flist[fi];
-    long long ustart = eoff[fi], uend = eoff[fi + 1];
-    int ubeg = __ldg(&nindex[u]);
-    u64 cm = changed[u];
-    int du0 = dist[(long long)u * kLanes + lane], du1 = dist[(long long)u * kLanes + 32 + lane];
-    for (long long k = c0; k < c1; k++) {
-      while (k >= uend) {
-        fi++;
-        u = flist[fi];
-        ustart = uend;
-        uend = eoff[fi + 1];
-        ubeg = __ldg(&nindex[u]);
-        cm = changed[u];
-        du0 = dist[(long long)u * kLanes + lane];
-        du1 = dist[(long long)u * kLanes + 32 + lane];
-      }
-      const int e = ubeg + (int)(k - ustart);
-      const int v = __ldg(&nlist[e]);
-      const int w = __ldg(&eweight[e]);
-      bool imp0 = false, imp1 = false;
-      if ((cm >> lane) & 1ull) {
-        const long long nd = (long long)du0 + w;
-        int* p = &dist[(long long)v * kLanes + lane];
-        imp0 = nd < *p && atomicMin(p, (int)nd) > (int)nd;
-      }
-      if ((cm >> (32 + lane)) & 1ull) {
-        const long long nd = (long long)du1 + w;
-        int* p = &dist[(long long)v * kLanes + 32 + lane];
-        imp1 = nd < *p && atomicMin(p, (int)nd) > (int)nd;
-      }
-      improved[0] += imp0;
-      improved[1] += imp1;
-      const u64 bits = (u64)__ballot_sync(IG_FULL, imp0) | ((u64)__ballot_sync(IG_FULL, imp1) << 32);
-      if (bits) {
-        bool first = false;
-        if (lane == 0) first = atomicOr(&changed_next[v], bits) == 0ull;
-        if (__shfl_sync(IG_FULL, first, 0)) {
-          if (lane == pending) my_push = v;
-          if (++pending == 32) flush();
+    long long k = c0;
+    while (k < c1) {  // one frontier vertex's part of the chunk at a time (warp-uniform)
+      while (k >= eoff[fi + 1]) fi++;
+      const int u = flist[fi];
+      const long long s1 = min(c1, (long long)eoff[fi + 1]);
+      const int ubeg = __ldg(&nindex[u]) + (int)(k - eoff[fi]);
+      const u64 cm = changed[u];
+      const int kl = __popcll(cm);
+      const int pairs = (int)(s1 - k) * kl;
+      for (int pb = 0; pb < pairs; pb += 32) {
+        const int p = pb + lane;
+        int item[1] = {0};
+        int na = 0;
+        if (p < pairs) {
+          const int eo = p / kl;
+          const int q = nth_set_bit(cm, p - eo * kl);
+          const int du = dist[(long long)u * kLanes + q];
+          if (du != kInf) {
+            const int e = ubeg + eo;
+            const int v = __ldg(&nlist[e]);
+            const long long nd = (long long)du + __ldg(&eweight[e]);
+            int* pv = &dist[(long long)v * kLanes + q];
+            if (nd < *pv && atomicMin(pv, (int)nd) > (int)nd) {
+              imp_lanes |= 1ull << q;
+              if (atomicOr(&changed_next[v], 1ull << q) == 0ull) {
+                item[0] = v;
+                na = 1;
+              }
+            }
+          }
         }
+        warp_buf_append<1>(na, item, buf, nbuf, tlist, tsize, n, ctl);
       }
+      k = s1;
     }
   }
-  flush();
-  if (improved[0]) atomicAdd(&st->cnt[lane], improved[0]);
-  if (improved[1]) atomicAdd(&st->cnt[32 + lane], improved[1]);
+  warp_buf_flush(buf, nbuf, tlist, tsize, n, ctl);
+  // a lane that improved nothing this round is finished
+  const unsigned lo_m = __reduce_or_sync(IG_FULL, (unsigned)imp_lanes);
+  const unsigned hi_m = __reduce_or_sync(IG_FULL, (unsigned)(imp_lanes >> 32));
+  if ((lo_m >> lane) & 1u) atomicAdd(&st->cnt[lane], 1ull);
+  if ((hi_m >> lane) & 1u) atomicAdd(&st->cnt[32 + lane], 1ull);
 }
 
 // Degree prefix of the frontier (for the edge-balanced round).
