@@ -10,11 +10,21 @@
 // hooking the larger root under the smaller one with atomicCAS, so a root is
 // the minimum of its tree; a final pass points every vertex at its root.
 // The result is the same min-id labelling in a number of passes independent
-// of the diameter.
+// of the diameter.  Most edges of a skewed graph never need a union: after
+// linking every vertex to its first kSample neighbours (neighbour sampling,
+// as in Afforest, Sutton et al. 2018) the largest component is already
+// connected, and only vertices outside it link their other edges (all of
+// them: the other end may be a skipped vertex; the graph is symmetric).
+// Every parent pointer goes to a smaller or equal id (init, larger-under-
+// smaller hooks, path halving), so each final root is its component's minimum.
 //
-//   init   : parent[v] = min(v, first neighbour)   (adjacency is sorted)
-//   hook   : for each edge (u, v) with v < u: union(u, v); vertices above the
-//            hub degree are deferred to an edge-balanced grid-wide pass
+//   init    : parent[v] = min(v, first neighbour)   (adjacency is sorted)
+//   sample  : union(v, neighbour r) for r = 0 .. kSample-1
+//   compress: parent[v] = root(v)
+//   giant   : the most frequent root among a fixed sample of vertices
+//   hook    : vertices whose root is not the giant one: union(v, w) for their
+//             neighbours from position kSample on; vertices above the hub
+//             degree are deferred to an edge-balanced grid-wide pass
 //   compress: label[v] = root(v)
 #include "ig_device.cuh"
 #include "ig_options.h"
@@ -22,6 +32,8 @@
 namespace {
 
 constexpr int kThreads = 256;
+constexpr int kSample = 2;      // neighbours linked before the giant component is picked
+constexpr int kGiantSamples = 1024;
 
 __device__ __forceinline__ int load_parent(const int* parent, int x) {
   return *((const volatile int*)parent + x);
@@ -69,28 +81,55 @@ __global__ void cc_init(const int* __restrict__ nindex, const int* __restrict__ 
   }
 }
 
+__global__ void cc_sample(const int* __restrict__ nindex, const int* __restrict__ nlist, int n, int* parent) {
+  for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < n; v += gridDim.x * blockDim.x) {
+    const int b = __ldg(&nindex[v]), e = __ldg(&nindex[v + 1]);
+    // position 0 too: init linked it only when the neighbour's id is smaller
+    for (int r = 0; r < kSample && b + r < e; r++) unite(parent, v, __ldg(&nlist[b + r]));
+  }
+}
+
+// The most frequent root among kGiantSamples evenly spaced vertices (parent
+// is compressed, so parent[x] is x's root); one block.  Written to ctl->i32[1].
+__global__ void __launch_bounds__(kThreads) cc_giant(const int* parent, int n, IgCtl* ctl) {
+  __shared__ int s_root[kGiantSamples];
+  __shared__ unsigned long long s_best;
+  const int m = n < kGiantSamples ? n : kGiantSamples;
+  for (int i = threadIdx.x; i < m; i += blockDim.x) s_root[i] = parent[(long long)i * n / m];
+  if (threadIdx.x == 0) s_best = 0;
+  __syncthreads();
+  for (int i = threadIdx.x; i < m; i += blockDim.x) {
+    int c = 0;
+    for (int j = 0; j < m; j++) c += s_root[j] == s_root[i];
+    // count in the high word, the smaller root wins ties (deterministic)
+    atomicMax(&s_best, ((unsigned long long)c << 32) | (unsigned)(0x7fffffff - s_root[i]));
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) ctl->i32[1] = 0x7fffffff - (int)(s_best & 0xffffffffu);
+}
+
 __global__ void __launch_bounds__(kThreads) cc_hook(const int* __restrict__ nindex, const int* __restrict__ nlist,
                                                     int n, int* parent, int* hubs, IgCtl* ctl, int hub_degree) {
   using namespace ig;
   const int lane = lane_id();
   const long long gtid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   const long long gthreads = (long long)gridDim.x * blockDim.x;
+  const int giant = ctl->i32[1];
   for (long long base = gtid & ~31LL; base < n; base += gthreads) {
     const long long v = base + lane;
     int beg = 0, deg = 0;
-    if (v < n) {
-      beg = __ldg(&nindex[v]);
-      deg = __ldg(&nindex[v + 1]) - beg;
+    // a vertex still pointing at the giant root is in the giant component:
+    // its edges to other components are linked from their other ends
+    if (v < n && load_parent(parent, (int)v) != giant) {
+      beg = __ldg(&nindex[v]) + kSample;
+      deg = max(0, __ldg(&nindex[v + 1]) - beg);
     }
     const bool hub = deg > hub_degree;
     warp_append(hub, (int)v, hubs, &ctl->i32[0], n, ctl);
     const int vv = (int)v;
     warp_expand(beg, hub ? 0 : deg, [&](bool act, int e, int j) {
       const int u = __shfl_sync(IG_FULL, vv, j);
-      if (act) {
-        const int w = __ldg(&nlist[e]);
-        if (w < u) unite(parent, u, w);
-      }
+      if (act) unite(parent, u, __ldg(&nlist[e]));
     });
   }
 }
@@ -102,10 +141,7 @@ __global__ void __launch_bounds__(kThreads) cc_hook_hubs(const int* __restrict__
   const int nh = ctl->i32[0];
   if (nh == 0) return;
   grid_expand_hubs(nindex, hubs, nh, [&](bool act, int e, int hv) {
-    if (act) {
-      const int w = __ldg(&nlist[e]);
-      if (w < hv) unite(parent, hv, w);
-    }
+    if (act) unite(parent, hv, __ldg(&nlist[e]));
   });
 }
 
@@ -148,10 +184,13 @@ int igk_cc(IgExec* ex, const ig_csr* dg, int* d_label) {
   const int grid_v = std::min((n + kThreads - 1) / kThreads, ex->sms * 16);
   const int grid_w = std::max(1, std::min((n + kThreads - 1) / kThreads, ex->sms * 8));
   cc_init<<<grid_v, kThreads, 0, ex->stream>>>(dg->nindex, dg->nlist, n, d_label);
+  cc_sample<<<grid_v, kThreads, 0, ex->stream>>>(dg->nindex, dg->nlist, n, d_label);
+  cc_compress<<<grid_v, kThreads, 0, ex->stream>>>(d_label, n);
+  cc_giant<<<1, kThreads, 0, ex->stream>>>(d_label, n, ex->d_ctl);
   cc_hook<<<grid_w, kThreads, 0, ex->stream>>>(dg->nindex, dg->nlist, n, d_label, (int*)hubs, ex->d_ctl,
                                                o.hub_degree);
   cc_hook_hubs<<<ex->sms * 4, kThreads, 0, ex->stream>>>(dg->nindex, dg->nlist, d_label, (int*)hubs, ex->d_ctl);
   cc_compress<<<grid_v, kThreads, 0, ex->stream>>>(d_label, n);
-  ig_count_launches(4);
+  ig_count_launches(7);
   return ig_cuda_check((int)cudaGetLastError(), "cc launch");
 }
