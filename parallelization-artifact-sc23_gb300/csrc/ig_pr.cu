@@ -41,6 +41,7 @@ struct PrArgs {
   float* cb;
   int* hubs;          // hub vertices in increasing id order
   int* chunk_base;    // first chunk of each hub (hubs + 1 entries)
+  int* chunk_hub;     // hub index of each chunk
   float2* partial;    // per-chunk (hi, lo) sums
   int* blk;           // per-block counts for the deterministic hub compaction (2 * grid)
   double* blkerr;     // per-block residual partials (2 * grid)
@@ -208,6 +209,10 @@ __global__ void __launch_bounds__(kThreads) pr_persistent(PrArgs a) {
   if (!grid_sync(ctl, a.timeout_ns)) return;
   const int nh = ld_relaxed(&ctl->i32[10]);
   const int nchunks = ld_relaxed(&ctl->i32[11]);
+  // chunk -> hub map, so a chunk finds its hub with one load every iteration
+  for (int h = warp_g; h < nh; h += nwarps)
+    for (int c = a.chunk_base[h] + lane; c < a.chunk_base[h + 1]; c += 32) a.chunk_hub[c] = h;
+  if (!grid_sync(ctl, a.timeout_ns)) return;
 
   float* cur = a.ca;
   float* nxt = a.cb;
@@ -227,13 +232,7 @@ __global__ void __launch_bounds__(kThreads) pr_persistent(PrArgs a) {
     auto frozen = [&](int g) { return kBatched && it > 1 && ld_relaxed(&gprev[g]) < (double)a.eps; };
     // ---- phase A: hub chunks (partial sums) and regular vertices
     for (int c = warp_g; c < nchunks; c += nwarps) {
-      // owning hub: largest h with chunk_base[h] <= c
-      int lo = 0, hi = nh - 1;
-      while (lo < hi) {
-        const int mid = (lo + hi + 1) >> 1;
-        if (a.chunk_base[mid] <= c) lo = mid;
-        else hi = mid - 1;
-      }
+      const int lo = a.chunk_hub[c];  // owning hub
       const int hv = a.hubs[lo];
       if (kBatched && frozen(graph_of(a, hv))) continue;
       const int hb = __ldg(&a.nindex[hv]), he = __ldg(&a.nindex[hv + 1]);
@@ -389,13 +388,14 @@ static int pr_launch(IgExec* ex, const ig_csr* dg, const int* d_degree, float* d
   const long long max_hubs = (long long)dg->edges / (hub_degree + 1) + 1;
   const long long max_chunks = (long long)dg->edges / chunk + max_hubs + 1;
   const int max_blocks = ex->sms * 32;
-  void *ca, *cb, *hubs, *cbase, *part, *blk, *blkerr, *gres = nullptr;
+  void *ca, *cb, *hubs, *cbase, *chub, *part, *blk, *blkerr, *gres = nullptr;
   int rc;
   if ((rc = ig_scratch_get(ex->scratch, IG_SLOT_F0, (size_t)n * sizeof(float), &ca))) return rc;
   if ((rc = ig_scratch_get(ex->scratch, IG_SLOT_F1, (size_t)n * sizeof(float), &cb))) return rc;
   if ((rc = ig_scratch_get(ex->scratch, IG_SLOT_Q0, (size_t)max_hubs * sizeof(int), &hubs))) return rc;
   if ((rc = ig_scratch_get(ex->scratch, IG_SLOT_Q1, (size_t)(max_hubs + 1) * sizeof(int), &cbase))) return rc;
   if ((rc = ig_scratch_get(ex->scratch, IG_SLOT_Q2, (size_t)max_chunks * sizeof(float2), &part))) return rc;
+  if ((rc = ig_scratch_get(ex->scratch, IG_SLOT_Q3, (size_t)max_chunks * sizeof(int), &chub))) return rc;
   if ((rc = ig_scratch_get(ex->scratch, IG_SLOT_V0, (size_t)2 * max_blocks * sizeof(int), &blk))) return rc;
   if ((rc = ig_scratch_get(ex->scratch, IG_SLOT_BLK, (size_t)2 * max_blocks * sizeof(double), &blkerr))) return rc;
   if (d_graph_vptr) {
@@ -409,7 +409,7 @@ static int pr_launch(IgExec* ex, const ig_csr* dg, const int* d_degree, float* d
   const float damp = 0.85f;
   const float base = (1.0f - damp) / (float)n;
   PrArgs a{dg->nindex, dg->nlist, d_degree, n, dg->edges, d_scores, (float*)ca, (float*)cb, (int*)hubs,
-           (int*)cbase, (float2*)part, (int*)blk, (double*)blkerr, ex->d_ctl, epsilon, max_iter, base, damp,
+           (int*)cbase, (int*)chub, (float2*)part, (int*)blk, (double*)blkerr, ex->d_ctl, epsilon, max_iter, base, damp,
            ex->timeout_ns, hub_degree, chunk, d_graph_vptr, graphs, (double*)gres, d_iters};
   void* args[] = {&a};
   const int cap = o.blocks_per_sm > 0 ? std::min(o.blocks_per_sm, 32) : 32;
