@@ -641,7 +641,7 @@ IgOptions& ig_options() {
       /*sssp_delta=*/0,
       /*sssp_delta_scale=*/128,
       /*sssp_heavy_split=*/0,
-      /*sssp_hub_degree=*/512,
+      /*sssp_hub_degree=*/1024,
       /*pr_hub_degree=*/1024,
       /*pr_chunk=*/4096,
   };

@@ -56,6 +56,7 @@ struct SsspArgs {
 // ctl->i32[k % 3]  size of the near queue processed by near iteration k
 // ctl->i32[3 + s]  hub count of near iteration with s = k % 3
 // ctl->i32[6 + f]  far-pile size of epoch with slot f = epoch % 3
+// ctl->i32[12 + s] frontier chunks taken beyond the first one per warp, s = k % 3
 // ctl->u64[4 + f]  minimum pending distance of that epoch's pile
 // ctl->u64[0..1]   weight-sample sum / count, ctl->u64[2] bucket width
 // ctl->work        relaxations that improved a distance
@@ -124,6 +125,7 @@ __global__ void __launch_bounds__(kThreads, 4) sssp_persistent(SsspArgs a) {
       if (gtid == 0) {
         ctl->i32[(it + 2) % 3] = 0;
         ctl->i32[3 + (it + 1) % 3] = 0;
+        ctl->i32[12 + (it + 1) % 3] = 0;
         if (heavy) ctl->i32[9 + (mpass + 1) % 2] = 0;
       }
       int* qsize = &ctl->i32[(it + 1) % 3];
@@ -175,7 +177,11 @@ __global__ void __launch_bounds__(kThreads, 4) sssp_persistent(SsspArgs a) {
         warp_buf_append<4>(nn, nq, nbuf, nbuf_n, nxt, qsize, a.nodes, ctl);
         warp_buf_append<4>(nf, fq, fbuf, fbuf_n, far, fsize, a.nodes, ctl);
       };
-      for (int base = warp_g * 32; base < fcount; base += nwarps * 32) {
+      // first chunk by warp index, the rest taken from a per-round counter so
+      // that warps that drew light chunks take more (the round ends at the
+      // grid barrier, so the slowest warp sets its length)
+      int* grab = &ctl->i32[12 + it % 3];
+      for (int base = warp_g * 32; base < fcount;) {
         const int i = base + lane;
         int u = 0, beg = 0, deg = 0, du = kInf;
         bool expand = false;
@@ -210,6 +216,9 @@ __global__ void __launch_bounds__(kThreads, 4) sssp_persistent(SsspArgs a) {
           for (int k = 0; k < 4; k++) duj[k] = __shfl_sync(IG_FULL, du, j[k]);
           relax4(act, e, duj);
         });
+        int nb = 0;
+        if (lane == 0) nb = nwarps * 32 + atomicAdd(grab, 32);
+        base = __shfl_sync(IG_FULL, nb, 0);
       }
       warp_buf_flush(nbuf, nbuf_n, nxt, qsize, a.nodes, ctl);
       warp_buf_flush(fbuf, fbuf_n, far, fsize, a.nodes, ctl);
