@@ -523,6 +523,54 @@ __device__ __forceinline__ void warp_buf_append(int cnt, const int (&items)[kMax
   }
 }
 
+// Writes out full groups of 32 buffered items (warp-uniform n).
+__device__ __forceinline__ void warp_buf_drain(int* buf, int& n, int* q, int* qsize, int cap, IgCtl* ctl) {
+  const int lane = lane_id();
+  while (n >= 32) {
+    int base = 0;
+    if (lane == 0) base = atomicAdd(qsize, 32);
+    base = __shfl_sync(IG_FULL, base, 0);
+    const int v = buf[lane];
+    if (base + lane < cap) q[base + lane] = v;
+    else raise(ctl, IG_ERR_OVERFLOW);
+    __syncwarp();
+    for (int i = 32 + lane; i < n; i += 32) buf[i - 32] = buf[i];
+    __syncwarp();
+    n -= 32;
+  }
+}
+
+// Two warp_buf_append calls for two queues in one: the per-lane counts of
+// both (at most kMax each, so a warp's total fits in 16 bits) are scanned
+// together, and a warp with nothing to append returns after one ballot.
+template <int kMax>
+__device__ __forceinline__ void warp_buf_append2(int c1, const int (&i1)[kMax], int* b1, int& n1, int* q1, int* s1,
+                                                 int c2, const int (&i2)[kMax], int* b2, int& n2, int* q2, int* s2,
+                                                 int cap, IgCtl* ctl) {
+  if (__ballot_sync(IG_FULL, (c1 | c2) != 0) == 0) return;
+  const int lane = lane_id();
+  const int packed = c1 | (c2 << 16);
+  int incl = packed;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int t = __shfl_up_sync(IG_FULL, incl, o);
+    if (lane >= o) incl += t;
+  }
+  const int total = __shfl_sync(IG_FULL, incl, 31);
+  const int ex = incl - packed;
+  const int p1 = n1 + (ex & 0xffff), p2 = n2 + (ex >> 16);
+#pragma unroll
+  for (int k = 0; k < kMax; k++) {
+    if (k < c1) b1[p1 + k] = i1[k];
+    if (k < c2) b2[p2 + k] = i2[k];
+  }
+  n1 += total & 0xffff;
+  n2 += total >> 16;
+  __syncwarp();
+  warp_buf_drain(b1, n1, q1, s1, cap, ctl);
+  warp_buf_drain(b2, n2, q2, s2, cap, ctl);
+}
+
 __device__ __forceinline__ void warp_buf_flush(int* buf, int& n, int* q, int* qsize, int cap, IgCtl* ctl) {
   if (n == 0) return;  // warp-uniform
   const int lane = lane_id();

@@ -174,8 +174,7 @@ __global__ void __launch_bounds__(kThreads, 4) sssp_persistent(SsspArgs a) {
             }
           }
         }
-        warp_buf_append<4>(nn, nq, nbuf, nbuf_n, nxt, qsize, a.nodes, ctl);
-        warp_buf_append<4>(nf, fq, fbuf, fbuf_n, far, fsize, a.nodes, ctl);
+        warp_buf_append2<4>(nn, nq, nbuf, nbuf_n, nxt, qsize, nf, fq, fbuf, fbuf_n, far, fsize, a.nodes, ctl);
       };
       // first chunk by warp index, the rest taken from a per-round counter so
       // that warps that drew light chunks take more (the round ends at the
