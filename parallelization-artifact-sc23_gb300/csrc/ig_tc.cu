@@ -39,6 +39,7 @@ constexpr int kHashCap = 2048;    // block table slots (out-degree <= 1024 is ha
 constexpr int kBitWords = 256;    // block filter: 8192 bits, bit (w mod 8192) set for w in N+(v)
 constexpr int kWarpCap = 128;     // warp table slots (out-degree <= kBlockOut)
 constexpr int kWarpBitWords = 64; // warp filter: 2048 bits
+constexpr int kWarpList = 96;     // in-neighbour lists this long are walked by the whole warp
 
 // Work items of middle vertex v with `out` out-neighbours and `in`
 // in-neighbours: warp items of kChunk in-neighbours for a short N+(v), block
@@ -266,31 +267,49 @@ __device__ __forceinline__ unsigned long long probe_group(const int* __restrict_
     }
     ud = ue - ub;
   }
-  // four 32-probe slots per step: their list loads are issued together
+  // membership of w in N+(v): filter bit first (rejects most misses with one
+  // shared load), then the hash table or a binary search of N+(v)
+  auto probe = [&](int w) -> int {
+    if (hashed) {
+      if (((bits[(w >> 5) & (kBits - 1)] >> (w & 31)) & 1u) == 0) return 0;
+      unsigned h = hash_slot(w, mask);
+      while (true) {
+        const int t = tab[h];
+        if (t == w) return 1;
+        if (t == -1) return 0;
+        h = (h + 1) & mask;
+      }
+    }
+    return contains(out_list + vb, vd, w) ? 1 : 0;
+  };
+  // long lists: the whole warp walks one list at a time, 128 probes per step,
+  // with no per-slot owner search
+  unsigned longs = __ballot_sync(IG_FULL, ud >= kWarpList);
+  while (longs) {
+    const int l = __ffs(longs) - 1;
+    longs &= longs - 1;
+    const int lb = __shfl_sync(IG_FULL, ub, l), le = lb + __shfl_sync(IG_FULL, ud, l);
+    for (int base = lb; base < le; base += 128) {
+      int w[4];
+#pragma unroll
+      for (int k = 0; k < 4; k++) {
+        const int e = base + k * 32 + lane;
+        w[k] = e < le ? __ldg(&out_list[e]) : -1;
+      }
+#pragma unroll
+      for (int k = 0; k < 4; k++)
+        if (w[k] >= 0) local += probe(w[k]);
+    }
+  }
+  if (ud >= kWarpList) ud = 0;
+  // short lists: four 32-probe slots per step, load-balanced over the lanes
   warp_expand4(ub, ud, [&](const bool (&act)[4], const int (&e)[4], const int (&)[4]) {
     int w[4];
 #pragma unroll
     for (int k = 0; k < 4; k++) w[k] = act[k] ? __ldg(&out_list[e[k]]) : -1;
 #pragma unroll
-    for (int k = 0; k < 4; k++) {
-      if (!act[k]) continue;
-      if (hashed) {
-        // most probes miss: the filter rejects them with one shared load
-        if (((bits[(w[k] >> 5) & (kBits - 1)] >> (w[k] & 31)) & 1u) == 0) continue;
-        unsigned h = hash_slot(w[k], mask);
-        while (true) {
-          const int t = tab[h];
-          if (t == w[k]) {
-            local++;
-            break;
-          }
-          if (t == -1) break;
-          h = (h + 1) & mask;
-        }
-      } else if (contains(out_list + vb, vd, w[k])) {
-        local++;
-      }
-    }
+    for (int k = 0; k < 4; k++)
+      if (act[k]) local += probe(w[k]);
   });
   return local;
 }
