@@ -119,6 +119,10 @@ int ig_csr_upload(const ig_csr* h, ig_csr* d);
 int ig_csr_free_device(ig_csr* d);
 /* CUDA events and streams as opaque handles. */
 int ig_stream_create(void** stream);
+/* A stream that is not ordered with the legacy default stream (host code must
+ * order its work with events or synchronize calls): for copies that should
+ * overlap the synchronous drop-in calls. */
+int ig_stream_create_nonblocking(void** stream);
 int ig_stream_destroy(void* stream);
 int ig_stream_synchronize(void* stream);
 int ig_event_create(void** ev);

@@ -287,6 +287,13 @@ extern "C" int ig_stream_create(void** s) {
   IG_CU(cudaStreamCreate((cudaStream_t*)s));
   return IG_OK;
 }
+extern "C" int ig_stream_create_nonblocking(void** s) {
+  if (!s) return ig_fail(IG_ERR_INVALID_ARG, "null");
+  // not ordered with the legacy default stream: copies on it overlap the
+  // synchronous drop-in calls (whose result copies use that stream)
+  IG_CU(cudaStreamCreateWithFlags((cudaStream_t*)s, cudaStreamNonBlocking));
+  return IG_OK;
+}
 extern "C" int ig_stream_destroy(void* s) {
   IG_CU(cudaStreamDestroy((cudaStream_t)s));
   return IG_OK;

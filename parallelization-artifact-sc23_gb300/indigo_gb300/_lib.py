@@ -112,6 +112,7 @@ SIGNATURES = {
     "ig_csr_free_device": (_I, [_PCSR]),
     "ig_stream_create": (_I, [ctypes.POINTER(_P)]),
     "ig_stream_destroy": (_I, [_P]),
+    "ig_stream_create_nonblocking": (_I, [ctypes.POINTER(_P)]),
     "ig_stream_synchronize": (_I, [_P]),
     "ig_event_create": (_I, [ctypes.POINTER(_P)]),
     "ig_event_destroy": (_I, [_P]),
