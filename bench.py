@@ -264,6 +264,23 @@ def run_ours(args, dist: Dist):
                 "algorithmic_bytes_per_launch": abytes[dom], "share_of_step": round(shares[dom], 4),
                 "timing": "CUDA events around each call on the launching stream, averaged over the timed steps"}
 
+    # Random-access ceiling: SSSP and PageRank are bound by data-dependent
+    # 4-byte reads of per-vertex arrays (one 32-byte sector each), so they are
+    # also reported against the device's measured rate of such reads.
+    gps = ig.probe_random_gather(V, 1 << 29, 3)
+    relaxed = []
+    for s in sources:  # edges expanded per SSSP call (one random distance read each)
+        G.sssp(int(s), dist_buf)
+        relaxed.append(G.last_run().aux[2])
+    sssp_rate = float(np.mean(relaxed)) / (per["sssp"]["ms_per_call"] * 1e-3)
+    pr_rate = E * pr_iters / (per["pr"]["ms_per_call"] * 1e-3)
+    random_access = {"unit": "random 4-byte reads/s", "peak": round(gps, -6),
+                     "peak_source": "measured now: ig_probe_random_gather, V-float table (L2-resident), 8 reads "
+                                    "in flight per thread",
+                     "sssp_reads_per_call": int(np.mean(relaxed)), "sssp": round(sssp_rate, -6),
+                     "sssp_frac": round(sssp_rate / gps, 4), "pr_reads_per_call": int(E * pr_iters),
+                     "pr": round(pr_rate, -6), "pr_frac": round(pr_rate / gps, 4)}
+
     e2e = None
     if not args.no_e2e:
         e2e = run_e2e(ig, g, gd, sources, args, dist)
@@ -286,7 +303,7 @@ def run_ours(args, dist: Dist):
                    "tc_input": "degree-ordered relabelling", "runs_per_step": RUNS_PER_STEP,
                    "l2": "inputs larger than L2 (nlist+eweight %.0f MB > 129 MB)" % (8 * E / 1e6),
                    "parallelism": "replicas" if dist.world > 1 else "single GPU"},
-        "e2e": e2e, "roofline": roofline, "cpu_baseline": cpu, "clocks": clk, "gpu_launches": launches,
+        "e2e": e2e, "roofline": roofline, "random_access": random_access, "cpu_baseline": cpu, "clocks": clk, "gpu_launches": launches,
         "per_algo": per, "validation": validation,
     }
     return out
@@ -585,7 +602,8 @@ def run_batched(args, dist: Dist):
         t1 = time.time()
         tune_ms = b.autotune(("bfs", "cc", "pr"), reps=2)
         tuned = {a: {"ms": round(tune_ms[a], 3),
-                     "options": {k: b.get_option(a, k) for k in ("blocks_per_sm", "hub_degree", "pr_hub_degree")}}
+                     "options": {k: b.get_option(a, k) for k in ("blocks_per_sm", "hub_degree", "pr_hub_degree",
+                                                                  "pr_blocks_per_sm")}}
                  for a in tune_ms}
         log(f"[bench] autotuned in {time.time() - t1:.1f}s: {tuned}")
     for _ in range(args.warmup):

@@ -185,7 +185,7 @@ int ig_pr(const ig_csr* h_g, float* h_scores, const int* h_degree,
 int ig_tc_vertex(long long* count, int nodes, const int* d_nindex,
                  const int* d_nlist, double* seconds);
 
-/* Edge-centric forms (include/*_edge_cuda.h).  sp is the COO source array
+/* Edge-centric forms (include/<algo>_edge_cuda.h).  sp is the COO source array
  * the reference drivers build (sp[e] = source vertex of edge e); residency as
  * in the reference: host for BFS/SSSP/CC (e.g. include/sssp_edge_cuda.h:60,
  * 149-155), device for MIS (include/mis_edge_cuda.h:154-161) and TC
@@ -328,6 +328,12 @@ int ig_server_destroy(ig_server* s);
 /* ---------------------------------------------------------------------------
  * Self-test (no counterpart in the reference, whose waits are host-side)
  * ------------------------------------------------------------------------ */
+/* Calibration (no reference counterpart): rate of random 4-byte reads of a
+ * table of table_elems floats (< 2^32), `gathers` reads per run, best of
+ * `reps` runs, in reads per second.  A table the size of a per-vertex array
+ * stays in L2, one larger than L2 is read from HBM.  It is the ceiling of the
+ * graph kernels' data-dependent reads (each moves a 32-byte sector). */
+int ig_probe_random_gather(long long table_elems, long long gathers, int reps, double* gathers_per_s);
 /* Launches a persistent kernel in which one block never reaches the grid
  * barrier and reports, in *observed_status, the status the others' bounded
  * wait produced (IG_ERR_TIMEOUT when the bound works). */

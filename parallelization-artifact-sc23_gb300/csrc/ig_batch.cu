@@ -235,7 +235,10 @@ std::vector<IgOptions> batch_variants(int algo, const IgOptions& base) {
   std::vector<IgOptions> out;
   auto add = [&](int bps, int hub, int pr_hub) {
     IgOptions o = base;
-    if (bps >= 0) o.blocks_per_sm = bps;
+    if (bps >= 0) {
+      if (algo == kPr) o.pr_blocks_per_sm = bps;  // PageRank has its own block count
+      else o.blocks_per_sm = bps;
+    }
     if (hub > 0) o.hub_degree = hub;
     if (pr_hub > 0) o.pr_hub_degree = pr_hub;
     out.push_back(o);
@@ -247,7 +250,7 @@ std::vector<IgOptions> batch_variants(int algo, const IgOptions& base) {
   } else if (algo == kCc) {
     for (int hub : {64, 256, 1024, 4096}) add(-1, hub, 0);
   } else if (algo == kPr) {
-    for (int bps : {2, 4, 8})
+    for (int bps : {2, 3, 4, 8})
       for (int ph : {1024, 4096}) add(bps, 0, ph);
   }
   return out;  // TC: its launch shape follows the shared-memory tables; nothing to tune

@@ -12,6 +12,7 @@ struct IgOptions {
   int sssp_hub_degree;    // SSSP: degree above which a vertex is expanded by the whole grid
   int pr_hub_degree;      // PageRank: degree above which a vertex is split in chunks
   int pr_chunk;           // PageRank: edges per hub chunk
+  int pr_blocks_per_sm;   // PageRank: resident blocks per SM (0 = blocks_per_sm)
 };
 
 IgOptions& ig_options();

@@ -114,23 +114,69 @@ __device__ __forceinline__ void warp_pair_reduce(float& hi, float& lo) {
 
 // Kahan sum of contrib[nlist[k]] over k = b + lane, b + lane + 32, ... < e,
 // returned as a (hi, lo) pair reduced over the warp (same value in all lanes).
+// Each lane keeps 8 gathers in flight and loads the next 8 indices while the
+// current values arrive; the adds stay in the order k, k + 32, k + 64, ...
 __device__ __forceinline__ void warp_gather_sum(const int* __restrict__ nlist, const float* contrib, int b, int e,
                                                 float& hi, float& lo) {
+  constexpr int kDepth = 8;
   float s = 0.f, c = 0.f;
   int k = b + ig::lane_id();
-  for (; k + 96 < e; k += 128) {
-    const int n0 = __ldg(&nlist[k]), n1 = __ldg(&nlist[k + 32]);
-    const int n2 = __ldg(&nlist[k + 64]), n3 = __ldg(&nlist[k + 96]);
-    const float x0 = contrib[n0], x1 = contrib[n1], x2 = contrib[n2], x3 = contrib[n3];
-    kahan_add(s, c, x0);
-    kahan_add(s, c, x1);
-    kahan_add(s, c, x2);
-    kahan_add(s, c, x3);
+  int n[kDepth];
+#pragma unroll
+  for (int t = 0; t < kDepth; t++) n[t] = k + 32 * t < e ? __ldg(&nlist[k + 32 * t]) : 0;
+  while (k < e) {
+    float x[kDepth];
+#pragma unroll
+    for (int t = 0; t < kDepth; t++) x[t] = k + 32 * t < e ? contrib[n[t]] : 0.f;
+    const int kn = k + 32 * kDepth;
+#pragma unroll
+    for (int t = 0; t < kDepth; t++) n[t] = kn + 32 * t < e ? __ldg(&nlist[kn + 32 * t]) : 0;
+#pragma unroll
+    for (int t = 0; t < kDepth; t++)
+      if (k + 32 * t < e) kahan_add(s, c, x[t]);
+    k = kn;
   }
-  for (; k < e; k += 32) kahan_add(s, c, contrib[__ldg(&nlist[k])]);
   hi = s;
   lo = -c;
   warp_pair_reduce(hi, lo);
+}
+
+// warp_gather_sum for two vertices at once ([b1, e1) and [b2, e2)): their
+// gathers are issued together (4 in flight per lane for each), each with its
+// own Kahan sum in the same per-lane order as warp_gather_sum, so the results
+// are the same bits.
+__device__ __forceinline__ void warp_gather_sum2(const int* __restrict__ nlist, const float* contrib, int b1, int e1,
+                                                 int b2, int e2, float& hi1, float& lo1, float& hi2, float& lo2) {
+  constexpr int kDepth = 4;
+  float s1 = 0.f, c1 = 0.f, s2 = 0.f, c2 = 0.f;
+  int k1 = b1 + ig::lane_id(), k2 = b2 + ig::lane_id();
+  while (k1 < e1 || k2 < e2) {
+    int n1[kDepth], n2[kDepth];
+#pragma unroll
+    for (int t = 0; t < kDepth; t++) {
+      n1[t] = k1 + 32 * t < e1 ? __ldg(&nlist[k1 + 32 * t]) : 0;
+      n2[t] = k2 + 32 * t < e2 ? __ldg(&nlist[k2 + 32 * t]) : 0;
+    }
+    float x1[kDepth], x2[kDepth];
+#pragma unroll
+    for (int t = 0; t < kDepth; t++) {
+      x1[t] = k1 + 32 * t < e1 ? contrib[n1[t]] : 0.f;
+      x2[t] = k2 + 32 * t < e2 ? contrib[n2[t]] : 0.f;
+    }
+#pragma unroll
+    for (int t = 0; t < kDepth; t++) {
+      if (k1 + 32 * t < e1) kahan_add(s1, c1, x1[t]);
+      if (k2 + 32 * t < e2) kahan_add(s2, c2, x2[t]);
+    }
+    k1 += 32 * kDepth;
+    k2 += 32 * kDepth;
+  }
+  hi1 = s1;
+  lo1 = -c1;
+  hi2 = s2;
+  lo2 = -c2;
+  warp_pair_reduce(hi1, lo1);
+  warp_pair_reduce(hi2, lo2);
 }
 
 __device__ __forceinline__ int vdegree(const PrArgs& a, int v) {
@@ -289,13 +335,20 @@ __global__ void __launch_bounds__(kThreads) pr_persistent(PrArgs a) {
         sum = __fsub_rn(s, c);
       }
       unsigned med = __ballot_sync(IG_FULL, vi < a.nodes && !skip && d > kLight && d <= a.hub_degree);
+      // two medium vertices at a time, so short ones do not each pay a full
+      // gather latency in turn
       while (med) {
-        const int l = __ffs(med) - 1;
+        const int l1 = __ffs(med) - 1;
         med &= med - 1;
-        const int mb = __shfl_sync(IG_FULL, b, l), me = __shfl_sync(IG_FULL, e, l);
-        float shi, slo;
-        warp_gather_sum(a.nlist, cur, mb, me, shi, slo);
-        if (lane == l) sum = __fadd_rn(shi, slo);
+        const int l2 = med ? __ffs(med) - 1 : l1;
+        if (med) med &= med - 1;
+        const int mb1 = __shfl_sync(IG_FULL, b, l1), me1 = __shfl_sync(IG_FULL, e, l1);
+        int mb2 = __shfl_sync(IG_FULL, b, l2), me2 = __shfl_sync(IG_FULL, e, l2);
+        if (l2 == l1) me2 = mb2;  // no second vertex
+        float h1, o1, h2, o2;
+        warp_gather_sum2(a.nlist, cur, mb1, me1, mb2, me2, h1, o1, h2, o2);
+        if (lane == l1) sum = __fadd_rn(h1, o1);
+        if (l2 != l1 && lane == l2) sum = __fadd_rn(h2, o2);
       }
       double verr = 0.0;
       const bool upd = vi < a.nodes && !skip && d <= a.hub_degree;
@@ -412,7 +465,8 @@ static int pr_launch(IgExec* ex, const ig_csr* dg, const int* d_degree, float* d
            (int*)cbase, (int*)chub, (float2*)part, (int*)blk, (double*)blkerr, ex->d_ctl, epsilon, max_iter, base, damp,
            ex->timeout_ns, hub_degree, chunk, d_graph_vptr, graphs, (double*)gres, d_iters};
   void* args[] = {&a};
-  const int cap = o.blocks_per_sm > 0 ? std::min(o.blocks_per_sm, 32) : 32;
+  const int bps = o.pr_blocks_per_sm > 0 ? o.pr_blocks_per_sm : o.blocks_per_sm;
+  const int cap = bps > 0 ? std::min(bps, 32) : 32;
   const void* fn = d_graph_vptr ? (const void*)pr_persistent<true> : (const void*)pr_persistent<false>;
   return ig_launch_coop(ex, fn, kThreads, 0, cap, args, nullptr);
 }

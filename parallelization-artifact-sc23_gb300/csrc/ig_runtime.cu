@@ -651,6 +651,7 @@ IgOptions& ig_options() {
       /*sssp_hub_degree=*/1024,
       /*pr_hub_degree=*/1024,
       /*pr_chunk=*/4096,
+      /*pr_blocks_per_sm=*/3,
   };
   return o;
 }
@@ -669,6 +670,7 @@ static const OptField g_opt_fields[] = {
     IG_OPT(hub_degree, 32, INT_MAX),  IG_OPT(sssp_delta, 0, INT_MAX),  IG_OPT(sssp_delta_scale, 1, 1 << 20),
     IG_OPT(sssp_heavy_split, 0, 1),   IG_OPT(sssp_hub_degree, 32, INT_MAX),
     IG_OPT(pr_hub_degree, 32, INT_MAX), IG_OPT(pr_chunk, 32, 1 << 24),
+    IG_OPT(pr_blocks_per_sm, 0, 32),
 };
 
 extern "C" int ig_set_option(const char* name, long long value) {

@@ -9,7 +9,8 @@ from .graph import (DeviceBuffer, DeviceCSR, Graph, device_count, erdos_renyi, g
                     read_egr, rmat, road)
 from .dropin import (GPUbfs_edge, GPUbfs_vertex, GPUcc_edge, GPUcc_vertex, GPUmis_vertex,  # noqa: F401
                      GPUsssp_edge, GPUsssp_vertex, GPUtc_vertex, PR_GPU)
-from .device import (DeviceGraph, Event, create_stream, get_option, kernel_launches, set_option,  # noqa: F401
+from .device import (DeviceGraph, Event, create_stream, get_option, kernel_launches, probe_random_gather,  # noqa: F401
+                     set_option,  # noqa: F401
                      set_wait_timeout_ms)
 
 from .batch import Batch, gen_batch, pack, unpack  # noqa: F401

@@ -113,6 +113,7 @@ SIGNATURES = {
     "ig_stream_create": (_I, [ctypes.POINTER(_P)]),
     "ig_stream_destroy": (_I, [_P]),
     "ig_stream_create_nonblocking": (_I, [ctypes.POINTER(_P)]),
+    "ig_probe_random_gather": (_I, [ctypes.c_longlong, ctypes.c_longlong, _I, ctypes.POINTER(ctypes.c_double)]),
     "ig_stream_synchronize": (_I, [_P]),
     "ig_event_create": (_I, [ctypes.POINTER(_P)]),
     "ig_event_destroy": (_I, [_P]),

@@ -114,3 +114,11 @@ def create_stream():
 
 def set_wait_timeout_ms(ms: int):
     check(load().ig_set_wait_timeout_ms(int(ms)))
+
+
+def probe_random_gather(table_elems: int, gathers: int = 1 << 29, reps: int = 3) -> float:
+    """Random 4-byte reads per second from a table of table_elems floats
+    (ig_probe_random_gather): the ceiling of data-dependent graph reads."""
+    out = ctypes.c_double()
+    check(load().ig_probe_random_gather(table_elems, gathers, reps, ctypes.byref(out)))
+    return out.value

@@ -122,6 +122,7 @@ def test_autotune_keeps_results(ig, gpu, expected):
         assert b.get_option("bfs", "blocks_per_sm") in (ig.get_option("blocks_per_sm"), 2, 4, 8)
         assert b.get_option("cc", "hub_degree") in (ig.get_option("hub_degree"), 64, 256, 1024, 4096)
         assert b.get_option("pr", "pr_hub_degree") in (ig.get_option("pr_hub_degree"), 1024, 4096)
+        assert b.get_option("pr", "pr_blocks_per_sm") in (ig.get_option("pr_blocks_per_sm"), 2, 3, 4, 8)
         outs = run_batch(ig, b)
     for call, (dist, lab, cnt, sc, its) in enumerate(outs):
         for i, (e_dist, e_lab, e_tc, e_sc, e_it) in enumerate(expected):

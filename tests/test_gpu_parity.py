@@ -289,3 +289,12 @@ def test_repeated_calls_reuse_scratch(ig, orc, graphs):
             dist = np.empty(g.nodes, np.int32)
             ig.GPUbfs_vertex(0, d, dist)
             assert np.array_equal(dist, orc.bfs(g, 0))
+
+
+def test_random_gather_probe(ig, gpu):
+    """The calibration kernel runs and gives a finite positive rate; it
+    rejects tables beyond its 32-bit index range."""
+    rate = ig.probe_random_gather(1 << 20, 1 << 22, 1)
+    assert math.isfinite(rate) and rate > 0
+    with pytest.raises(ig.IndigoError):
+        ig.probe_random_gather(1 << 33, 1 << 20, 1)
