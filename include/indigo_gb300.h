@@ -117,6 +117,18 @@ int ig_device_synchronize(void);
 /* Copies a host CSR to new device arrays (d->nodes/edges set, eweight may be NULL). */
 int ig_csr_upload(const ig_csr* h, ig_csr* d);
 int ig_csr_free_device(ig_csr* d);
+/* Device-side preparation of a graph already on the device (no counterpart
+ * in the reference, which prepares its inputs offline): self loops dropped,
+ * duplicate edges merged (the smallest weight kept), every adjacency list
+ * sorted -- the input contract of the drivers (include/ECLgraph.h) and the
+ * triangle-counting precondition (include/tc_vertex_cuda.h:157-165).  Flags:
+ * IG_PREP_SYMMETRIZE adds the reverse of every edge (same weight);
+ * IG_PREP_DEGREE_ORDER relabels the vertices in ascending (degree, id) order
+ * as ig_degree_order does on the host.  *d_out receives new device arrays
+ * (free them with ig_csr_free_device); the input is not changed.  Synchronous;
+ * temporary device memory of about 26 bytes per (symmetrised) edge. */
+enum { IG_PREP_SYMMETRIZE = 1, IG_PREP_DEGREE_ORDER = 2 };
+int ig_csr_prepare(const ig_csr* d_in, int flags, ig_csr* d_out);
 /* CUDA events and streams as opaque handles. */
 int ig_stream_create(void** stream);
 /* A stream that is not ordered with the legacy default stream (host code must

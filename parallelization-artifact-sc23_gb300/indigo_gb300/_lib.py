@@ -110,6 +110,7 @@ SIGNATURES = {
     "ig_device_synchronize": (_I, []),
     "ig_csr_upload": (_I, [_PCSR, _PCSR]),
     "ig_csr_free_device": (_I, [_PCSR]),
+    "ig_csr_prepare": (_I, [_PCSR, _I, _PCSR]),
     "ig_stream_create": (_I, [ctypes.POINTER(_P)]),
     "ig_stream_destroy": (_I, [_P]),
     "ig_stream_create_nonblocking": (_I, [ctypes.POINTER(_P)]),

@@ -178,6 +178,36 @@ class DeviceCSR:
     def nlist_ptr(self) -> int:
         return ctypes.cast(self.c.nlist, ctypes.c_void_p).value
 
+    @classmethod
+    def _adopt(cls, c: CSR) -> "DeviceCSR":
+        """Wraps device arrays the library allocated (freed by close)."""
+        d = cls.__new__(cls)
+        d.host, d.c, d.nodes, d.edges = None, c, c.nodes, c.edges
+        return d
+
+    def prepare(self, symmetrize: bool = False, degree_order: bool = False) -> "DeviceCSR":
+        """ig_csr_prepare: a new device graph without self loops or duplicate
+        edges and with sorted lists; optionally symmetrised and relabelled in
+        (degree, id) order."""
+        out = CSR()
+        flags = (1 if symmetrize else 0) | (2 if degree_order else 0)
+        check(load().ig_csr_prepare(ctypes.byref(self.c), flags, ctypes.byref(out)))
+        return DeviceCSR._adopt(out)
+
+    def to_graph(self) -> Graph:
+        """Copies the device arrays back into a host Graph."""
+        L = load()
+        ni = np.empty(self.nodes + 1, np.int32)
+        nl = np.empty(max(1, self.edges), np.int32)
+        check(L.ig_memcpy(ni.ctypes.data, ctypes.cast(self.c.nindex, ctypes.c_void_p), ni.nbytes, 2))
+        check(L.ig_memcpy(nl.ctypes.data, ctypes.cast(self.c.nlist, ctypes.c_void_p), nl.nbytes, 2))
+        ew = None
+        if self.c.eweight:
+            ew = np.empty(max(1, self.edges), np.int32)
+            check(L.ig_memcpy(ew.ctypes.data, ctypes.cast(self.c.eweight, ctypes.c_void_p), ew.nbytes, 2))
+            ew = ew[: self.edges]
+        return Graph(ni, nl[: self.edges], ew)
+
     def close(self):
         if self.c.nindex:
             load().ig_csr_free_device(ctypes.byref(self.c))
