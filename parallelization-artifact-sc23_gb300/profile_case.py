@@ -3,8 +3,8 @@ on a synthetic RMAT graph (default scale 21: 2,097,152 vertices, about 63M
 directed edges, so the 250 MB neighbour list exceeds the 129 MB L2), run a
 few times through the device-resident API.
 
-    python parallelization-artifact-sc23_gb300/profile_case.py --algo bfs [--scale 21] [--repeat 3]
-           [--opt sssp_delta=100 ...]
+    python parallelization-artifact-sc23_gb300/profile_case.py --algo bfs [--scale 21 | --graph road:4096]
+           [--repeat 3] [--opt sssp_delta=100 ...]
 
 It prints one line per run with the CUDA-event time and the algorithmic
 bytes, so a capture can be related to the bench's roofline figures."""
@@ -25,13 +25,23 @@ def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--algo", choices=["bfs", "sssp", "cc", "mis", "pr", "tc"], required=True)
     ap.add_argument("--scale", type=int, default=21)
+    ap.add_argument("--graph", default="", help="instead of --scale: rmat:<scale> | road:<side> | grid:<side>")
     ap.add_argument("--repeat", type=int, default=3)
     ap.add_argument("--opt", action="append", default=[], help="kernel option name=value (ig_set_option)")
     args = ap.parse_args()
     for o in args.opt:
         name, value = o.split("=")
         ig.set_option(name, int(value))
-    g = ig.rmat(args.scale, 16, seed=7, maxw=1000)
+    if args.graph:
+        kind, _, arg = args.graph.partition(":")
+        if kind == "road":  # the high-diameter configuration: 5% of edges deleted, 0.1% shortcuts
+            g = ig.road(int(arg), int(arg), 0.05, 0.001, seed=11, maxw=10000)
+        elif kind == "grid":
+            g = ig.grid2d(int(arg), int(arg), maxw=255)
+        else:
+            g = ig.rmat(int(arg), 16, seed=7, maxw=1000)
+    else:
+        g = ig.rmat(args.scale, 16, seed=7, maxw=1000)
     if args.algo == "tc":
         g = g.degree_ordered()
     V, E = g.nodes, g.edges
