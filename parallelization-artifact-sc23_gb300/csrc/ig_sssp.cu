@@ -42,12 +42,14 @@ struct SsspArgs {
   int* stamp;    // near-queue membership stamp
   int* farflag;  // far-pile membership (epoch + 1)
   int* hubs;
+  int* mlist;     // per-round list of medium vertices (expanded one per warp)
   int* expanded;  // distance each vertex was last expanded with (INT_MAX: never)
   int* members;   // vertices light-expanded since the last heavy pass
   int* inmember;  // 1 while a vertex sits in members
   IgCtl* ctl;
   unsigned long long timeout_ns;
   int hub_degree;
+  int warp_degree;       // vertices with more neighbours than this (up to hub_degree) go to mlist
   long long delta;       // > 0: fixed bucket width
   int delta_scale;
   int heavy_split;       // 1: light/heavy edge split (heavy edges relaxed once per bucket)
@@ -57,6 +59,7 @@ struct SsspArgs {
 // ctl->i32[3 + s]  hub count of near iteration with s = k % 3
 // ctl->i32[6 + f]  far-pile size of epoch with slot f = epoch % 3
 // ctl->i32[12 + s] frontier chunks taken beyond the first one per warp, s = k % 3
+// ctl->i32[15 + s] medium-list size of near iteration k; ctl->i32[18 + s] its entries taken
 // ctl->u64[4 + f]  minimum pending distance of that epoch's pile
 // ctl->u64[0..1]   weight-sample sum / count, ctl->u64[2] bucket width
 // ctl->work        relaxations that improved a distance
@@ -126,6 +129,8 @@ __global__ void __launch_bounds__(kThreads, 4) sssp_persistent(SsspArgs a) {
         ctl->i32[(it + 2) % 3] = 0;
         ctl->i32[3 + (it + 1) % 3] = 0;
         ctl->i32[12 + (it + 1) % 3] = 0;
+        ctl->i32[15 + (it + 1) % 3] = 0;
+        ctl->i32[18 + (it + 1) % 3] = 0;
         if (heavy) ctl->i32[9 + (mpass + 1) % 2] = 0;
       }
       int* qsize = &ctl->i32[(it + 1) % 3];
@@ -204,12 +209,15 @@ __global__ void __launch_bounds__(kThreads, 4) sssp_persistent(SsspArgs a) {
         if (a.heavy_split && !heavy)
           warp_append(expand && atomicExch(&a.inmember[u], 1) == 0, u, a.members, nmembers, a.nodes, ctl);
         const bool hub = deg > a.hub_degree;
+        const bool medium = !hub && deg > a.warp_degree;
         warp_append(hub, u, a.hubs, nhub, a.nodes, ctl);
+        warp_append(medium, u, a.mlist, &ctl->i32[15 + it % 3], a.nodes, ctl);
         if (expand) {
           frontier_v++;
           frontier_e += deg;
         }
-        warp_expand4(beg, hub ? 0 : deg, [&](const bool (&act)[4], const int (&e)[4], const int (&j)[4]) {
+        // the chunk's short lists here: at most 32 * warp_degree edges per warp
+        warp_expand4(beg, (hub || medium) ? 0 : deg, [&](const bool (&act)[4], const int (&e)[4], const int (&j)[4]) {
           int duj[4];
 #pragma unroll
           for (int k = 0; k < 4; k++) duj[k] = __shfl_sync(IG_FULL, du, j[k]);
@@ -223,12 +231,42 @@ __global__ void __launch_bounds__(kThreads, 4) sssp_persistent(SsspArgs a) {
       warp_buf_flush(fbuf, fbuf_n, far, fsize, a.nodes, ctl);
       if (!grid_sync(ctl, a.timeout_ns)) return;
       const int nh = ld_relaxed(nhub);
-      if (nh > 0) {
+      const int nm = ld_relaxed(&ctl->i32[15 + it % 3]);
+      if (nh > 0 || nm > 0) {
         // hub distances are read once per staged hub; a hub improved since
         // was queued again and is expanded with its new distance next round
-        grid_expand_hubs4(
-            a.nindex, a.hubs, nh, [&](int v) { return a.dist[v]; },
-            [&](const bool (&act)[4], const int (&e)[4], const int (&)[4], const int (&du)[4]) { relax4(act, e, du); });
+        if (nh > 0)
+          grid_expand_hubs4(a.nindex, a.hubs, nh, [&](int v) { return a.dist[v]; },
+                            [&](const bool (&act)[4], const int (&e)[4], const int (&)[4], const int (&du)[4]) {
+                              relax4(act, e, du);
+                            });
+        // medium vertices, one whole warp each over its contiguous list (no
+        // owner search), four at a time taken from a counter after the first
+        // four by warp index, so warps that finished their hub share early
+        // take more
+        int* mgrab = &ctl->i32[18 + it % 3];
+        for (int m0 = warp_g * 4; m0 < nm;) {
+          for (int mi = m0; mi < min(m0 + 4, nm); mi++) {
+            const int u = a.mlist[mi];
+            const int du = a.dist[u];
+            const int b = __ldg(&a.nindex[u]), d = __ldg(&a.nindex[u + 1]) - b;
+            for (int base = 0; base < d; base += 128) {
+              bool act[4];
+              int e[4], duk[4];
+#pragma unroll
+              for (int k = 0; k < 4; k++) {
+                const int off = base + k * 32 + lane;
+                act[k] = off < d;
+                e[k] = b + (act[k] ? off : 0);
+                duk[k] = du;
+              }
+              relax4(act, e, duk);
+            }
+          }
+          int nb = 0;
+          if (lane == 0) nb = nwarps * 4 + atomicAdd(mgrab, 4);
+          m0 = __shfl_sync(IG_FULL, nb, 0);
+        }
         warp_buf_flush(nbuf, nbuf_n, nxt, qsize, a.nodes, ctl);
         warp_buf_flush(fbuf, fbuf_n, far, fsize, a.nodes, ctl);
         if (!grid_sync(ctl, a.timeout_ns)) return;
@@ -306,7 +344,7 @@ __global__ void __launch_bounds__(kThreads, 4) sssp_persistent(SsspArgs a) {
 
 int igk_sssp(IgExec* ex, const ig_csr* dg, int src, int* d_dist) {
   const size_t vb = (size_t)dg->nodes * sizeof(int);
-  void *qa, *qb, *fa, *fb, *stamp, *farflag, *hubs;
+  void *qa, *qb, *fa, *fb, *stamp, *farflag, *hubs, *mlist;
   int rc;
   if ((rc = ig_scratch_get(ex->scratch, IG_SLOT_Q0, vb, &qa))) return rc;
   if ((rc = ig_scratch_get(ex->scratch, IG_SLOT_Q1, vb, &qb))) return rc;
@@ -315,6 +353,7 @@ int igk_sssp(IgExec* ex, const ig_csr* dg, int src, int* d_dist) {
   if ((rc = ig_scratch_get(ex->scratch, IG_SLOT_V0, vb, &stamp))) return rc;
   if ((rc = ig_scratch_get(ex->scratch, IG_SLOT_V1, vb, &farflag))) return rc;
   if ((rc = ig_scratch_get(ex->scratch, IG_SLOT_V2, vb, &hubs))) return rc;
+  if ((rc = ig_scratch_get(ex->scratch, IG_SLOT_G0, vb, &mlist))) return rc;
   void *expanded, *members, *inmember;
   if ((rc = ig_scratch_get(ex->scratch, IG_SLOT_F0, vb, &expanded))) return rc;
   if ((rc = ig_scratch_get(ex->scratch, IG_SLOT_F1, vb, &members))) return rc;
@@ -322,8 +361,9 @@ int igk_sssp(IgExec* ex, const ig_csr* dg, int src, int* d_dist) {
   if ((rc = ig_exec_reset(ex))) return rc;
   const IgOptions& o = ig_exec_options(ex);
   SsspArgs a{dg->nindex, dg->nlist, dg->eweight, dg->nodes, dg->edges, src, d_dist,
-             (int*)qa, (int*)qb, (int*)fa, (int*)fb, (int*)stamp, (int*)farflag, (int*)hubs,
+             (int*)qa, (int*)qb, (int*)fa, (int*)fb, (int*)stamp, (int*)farflag, (int*)hubs, (int*)mlist,
              (int*)expanded, (int*)members, (int*)inmember, ex->d_ctl, ex->timeout_ns, o.sssp_hub_degree,
+             o.sssp_warp_degree,
              o.sssp_delta, o.sssp_delta_scale, o.sssp_heavy_split};
   void* args[] = {&a};
   return ig_launch_coop(ex, (const void*)sssp_persistent, kThreads, 0, o.blocks_per_sm, args, nullptr);
