@@ -14,6 +14,7 @@ struct IgOptions {
   int pr_hub_degree;      // PageRank: degree above which a vertex is split in chunks
   int pr_chunk;           // PageRank: edges per hub chunk
   int pr_blocks_per_sm;   // PageRank: resident blocks per SM (0 = blocks_per_sm)
+  int tc_block_chunk;     // TC: in-neighbours per block work item
 };
 
 IgOptions& ig_options();

@@ -653,6 +653,7 @@ IgOptions& ig_options() {
       /*pr_hub_degree=*/1024,
       /*pr_chunk=*/4096,
       /*pr_blocks_per_sm=*/3,
+      /*tc_block_chunk=*/4096,
   };
   return o;
 }
@@ -671,7 +672,7 @@ static const OptField g_opt_fields[] = {
     IG_OPT(hub_degree, 32, INT_MAX),  IG_OPT(sssp_delta, 0, INT_MAX),  IG_OPT(sssp_delta_scale, 1, 1 << 20),
     IG_OPT(sssp_heavy_split, 0, 1),   IG_OPT(sssp_hub_degree, 32, INT_MAX), IG_OPT(sssp_warp_degree, 1, INT_MAX),
     IG_OPT(pr_hub_degree, 32, INT_MAX), IG_OPT(pr_chunk, 32, 1 << 24),
-    IG_OPT(pr_blocks_per_sm, 0, 32),
+    IG_OPT(pr_blocks_per_sm, 0, 32), IG_OPT(tc_block_chunk, 256, 1 << 16),
 };
 
 extern "C" int ig_set_option(const char* name, long long value) {

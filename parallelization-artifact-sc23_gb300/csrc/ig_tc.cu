@@ -34,7 +34,6 @@ constexpr int kWarps = kThreads / 32;
 constexpr int kOrientHub = 256;   // lists longer than this are split by one block each
 constexpr int kBlockOut = 64;     // middle vertices with more out-neighbours are counted by whole blocks
 constexpr int kChunk = 64;        // in-neighbours per warp work item
-constexpr int kBlockChunk = 1024; // in-neighbours per block work item
 constexpr int kHashCap = 2048;    // block table slots (out-degree <= 1024 is hashed)
 constexpr int kBitWords = 256;    // block filter: 8192 bits, bit (w mod 8192) set for w in N+(v)
 constexpr int kWarpCap = 128;     // warp table slots (out-degree <= kBlockOut)
@@ -43,17 +42,18 @@ constexpr int kWarpList = 96;     // in-neighbour lists this long are walked by 
 
 // Work items of middle vertex v with `out` out-neighbours and `in`
 // in-neighbours: warp items of kChunk in-neighbours for a short N+(v), block
-// items of kBlockChunk for a long one (the block shares one table of N+(v)).
-__device__ __forceinline__ void tc_items(int out, int in, int* warp_items, int* block_items) {
+// items of `block_chunk` for a long one (the block shares one table of N+(v)).
+__device__ __forceinline__ void tc_items(int out, int in, int block_chunk, int* warp_items, int* block_items) {
   *warp_items = (out > 0 && out <= kBlockOut) ? (in + kChunk - 1) / kChunk : 0;
-  *block_items = out > kBlockOut ? (in + kBlockChunk - 1) / kBlockChunk : 0;
+  *block_items = out > kBlockOut ? (in + block_chunk - 1) / block_chunk : 0;
 }
 
 __device__ __forceinline__ bool before(int du, int u, int dw, int w) { return du < dw || (du == dw && u < w); }
 
 __global__ void __launch_bounds__(kThreads) tc_orient_count(const int* __restrict__ nindex,
                                                             const int* __restrict__ nlist, int n, int* out_cnt,
-                                                            int* item_cnt, int* item_cnt_b, int* hubs, IgCtl* ctl) {
+                                                            int* item_cnt, int* item_cnt_b, int* hubs,
+                                                            int block_chunk, IgCtl* ctl) {
   using namespace ig;
   __shared__ int s_cnt[kWarps][32];
   const int lane = lane_id(), wib = threadIdx.x >> 5;
@@ -92,7 +92,7 @@ __global__ void __launch_bounds__(kThreads) tc_orient_count(const int* __restric
     if (v < n && !hub) {
       const int oc = s_cnt[wib][lane];
       out_cnt[v] = oc;
-      tc_items(oc, deg - oc, &item_cnt[v], &item_cnt_b[v]);
+      tc_items(oc, deg - oc, block_chunk, &item_cnt[v], &item_cnt_b[v]);
     }
     __syncwarp();
   }
@@ -156,7 +156,7 @@ __global__ void __launch_bounds__(kThreads) tc_orient_fill(const int* __restrict
 __global__ void __launch_bounds__(kThreads) tc_orient_hubs_count(const int* __restrict__ nindex,
                                                                  const int* __restrict__ nlist, int n,
                                                                  const int* hubs, int* out_cnt, int* item_cnt,
-                                                                 int* item_cnt_b, IgCtl* ctl) {
+                                                                 int* item_cnt_b, int block_chunk, IgCtl* ctl) {
   using namespace ig;
   __shared__ int s_tmp[33];
   const int nh = ctl->i32[0];
@@ -175,7 +175,7 @@ __global__ void __launch_bounds__(kThreads) tc_orient_hubs_count(const int* __re
     block_scan_int(keep, s_tmp, &total);
     if (threadIdx.x == 0) {
       out_cnt[u] = total;
-      tc_items(total, du - total, &item_cnt[u], &item_cnt_b[u]);
+      tc_items(total, du - total, block_chunk, &item_cnt[u], &item_cnt_b[u]);
     }
     __syncthreads();
   }
@@ -401,7 +401,7 @@ __global__ void __launch_bounds__(kThreads) tc_count_warp(const int* __restrict_
   }
 }
 // Block work items: (middle vertex v with out-degree > kBlockOut, up to
-// kBlockChunk of its in-neighbours).  The block hashes N+(v) once into one
+// block_chunk of its in-neighbours).  The block hashes N+(v) once into one
 // shared table (9 KB instead of a 9 KB table per warp, so eight blocks fit
 // on an SM) and its warps take groups of 32 in-neighbours from a shared
 // counter until the item is done.
@@ -413,7 +413,8 @@ __global__ void __launch_bounds__(kThreads, 8) tc_count_block(const int* __restr
                                                               const int* __restrict__ item_off,
                                                               const int* __restrict__ item_v, int n,
                                                               unsigned long long* count, const IgCtl* ctl,
-                                                              const int* __restrict__ graph_vptr, int graphs) {
+                                                              const int* __restrict__ graph_vptr, int graphs,
+                                                              int block_chunk) {
   using namespace ig;
   __shared__ int tab[kHashCap];
   __shared__ unsigned bits[kBitWords];
@@ -453,8 +454,8 @@ __global__ void __launch_bounds__(kThreads, 8) tc_count_block(const int* __restr
     __syncthreads();
     const int ib = __ldg(&nindex[v]) - vb;  // in_off[v]
     const int iend = __ldg(&nindex[v + 1]) - __ldg(&out_off[v + 1]);
-    const int c0 = ib + (it - __ldg(&item_off[v])) * kBlockChunk;
-    const int c1 = min(c0 + kBlockChunk, iend);
+    const int c0 = ib + (it - __ldg(&item_off[v])) * block_chunk;
+    const int c1 = min(c0 + block_chunk, iend);
     const unsigned long long before_item = local;
     while (true) {
       int g = 0;
@@ -490,6 +491,7 @@ int igk_tc_batched(IgExec* ex, int nodes, int edges, const int* d_nindex, const 
 static int tc_run(IgExec* ex, int nodes, int edges, const int* d_nindex, const int* d_nlist, unsigned long long* d_count,
                   const int* d_graph_vptr, int graphs) {
   const size_t vb = ((size_t)nodes + 1) * sizeof(int);
+  const int block_chunk = ig_exec_options(ex).tc_block_chunk;
   void *cnt, *off, *icnt, *ioff, *icnt_b, *ioff_b, *list, *inl, *hubs, *itemv, *itemv_b;
   int rc;
   if ((rc = ig_scratch_get(ex->scratch, IG_SLOT_V0, vb, &cnt))) return rc;
@@ -504,7 +506,7 @@ static int tc_run(IgExec* ex, int nodes, int edges, const int* d_nindex, const i
                            &itemv)))
     return rc;
   if ((rc = ig_scratch_get(ex->scratch, IG_SLOT_Q3,
-                           ((size_t)edges / kBlockChunk + (size_t)nodes + 1) * sizeof(int), &itemv_b)))
+                           ((size_t)edges / block_chunk + (size_t)nodes + 1) * sizeof(int), &itemv_b)))
     return rc;
   if ((rc = ig_scratch_get(ex->scratch, IG_SLOT_E0, std::max<size_t>(1, (size_t)edges) * sizeof(int), &list)))
     return rc;
@@ -517,9 +519,10 @@ static int tc_run(IgExec* ex, int nodes, int edges, const int* d_nindex, const i
     return rc;
   const int grid = std::max(1, std::min((nodes + kThreads - 1) / kThreads, ex->sms * 8));
   tc_orient_count<<<grid, kThreads, 0, ex->stream>>>(d_nindex, d_nlist, nodes, (int*)cnt, (int*)icnt, (int*)icnt_b,
-                                                      (int*)hubs, ex->d_ctl);
+                                                      (int*)hubs, block_chunk, ex->d_ctl);
   tc_orient_hubs_count<<<ex->sms * 8, kThreads, 0, ex->stream>>>(d_nindex, d_nlist, nodes, (const int*)hubs,
-                                                                 (int*)cnt, (int*)icnt, (int*)icnt_b, ex->d_ctl);
+                                                                 (int*)cnt, (int*)icnt, (int*)icnt_b, block_chunk,
+                                                                 ex->d_ctl);
   if ((rc = igk_exclusive_scan(ex, (const int*)cnt, (int*)off, nodes, nullptr))) return rc;
   if ((rc = igk_exclusive_scan(ex, (const int*)icnt, (int*)ioff, nodes, nullptr))) return rc;
   if ((rc = igk_exclusive_scan(ex, (const int*)icnt_b, (int*)ioff_b, nodes, nullptr))) return rc;
@@ -534,7 +537,7 @@ static int tc_run(IgExec* ex, int nodes, int edges, const int* d_nindex, const i
     tc_count_block<true><<<cgrid, kThreads, 0, ex->stream>>>((const int*)off, (const int*)list, d_nindex,
                                                              (const int*)inl, (const int*)ioff_b,
                                                              (const int*)itemv_b, nodes, d_count, ex->d_ctl,
-                                                             d_graph_vptr, graphs);
+                                                             d_graph_vptr, graphs, block_chunk);
     tc_count_warp<true><<<cgrid, kThreads, 0, ex->stream>>>((const int*)off, (const int*)list, d_nindex,
                                                             (const int*)inl, (const int*)ioff, (const int*)itemv,
                                                             nodes, d_count, ex->d_ctl, d_graph_vptr, graphs);
@@ -542,7 +545,7 @@ static int tc_run(IgExec* ex, int nodes, int edges, const int* d_nindex, const i
     tc_count_block<false><<<cgrid, kThreads, 0, ex->stream>>>((const int*)off, (const int*)list, d_nindex,
                                                               (const int*)inl, (const int*)ioff_b,
                                                               (const int*)itemv_b, nodes, d_count, ex->d_ctl,
-                                                              nullptr, 0);
+                                                              nullptr, 0, block_chunk);
     tc_count_warp<false><<<cgrid, kThreads, 0, ex->stream>>>((const int*)off, (const int*)list, d_nindex,
                                                              (const int*)inl, (const int*)ioff, (const int*)itemv,
                                                              nodes, d_count, ex->d_ctl, nullptr, 0);

@@ -37,12 +37,12 @@ AXES = {
     "cc": {"blocks_per_sm": [4, 8], "hub_degree": [256, 64, 4096]},
     "mis": {"blocks_per_sm": [4, 2, 8]},
     "pr": {"pr_blocks_per_sm": [3, 2, 4], "pr_hub_degree": [1024, 256, 4096], "pr_chunk": [4096, 512]},
-    "tc": {"blocks_per_sm": [4]},
+    "tc": {"tc_block_chunk": [4096, 1024]},
 }
 # short labels for the variant names (like the suite's style words)
 LABEL = {"blocks_per_sm": "B", "hub_degree": "Hub", "bfs_alpha": "Alpha", "sssp_hub_degree": "Hub",
          "sssp_warp_degree": "Warp", "sssp_delta_scale": "Delta", "sssp_heavy_split": "Split", "pr_blocks_per_sm": "B",
-         "pr_hub_degree": "Hub", "pr_chunk": "Chunk"}
+         "pr_hub_degree": "Hub", "pr_chunk": "Chunk", "tc_block_chunk": "Item"}
 
 
 def variants(algo: str) -> list:
@@ -127,7 +127,7 @@ def sweep(g, algos, repeat: int, graph_name: str, log=print) -> dict:
     gd = g.degree_ordered() if "tc" in algos else None
     src = int(g.pick_sources(1, seed=7)[0])
     names = ("blocks_per_sm", "hub_degree", "bfs_alpha", "sssp_hub_degree", "sssp_warp_degree", "sssp_delta_scale",
-             "sssp_heavy_split", "pr_blocks_per_sm", "pr_hub_degree", "pr_chunk")
+             "sssp_heavy_split", "pr_blocks_per_sm", "pr_hub_degree", "pr_chunk", "tc_block_chunk")
     saved = {k: ig.get_option(k) for k in names}
     rows = {}
     with ig.DeviceCSR(g) as d:
