@@ -309,28 +309,20 @@ __global__ void __launch_bounds__(kThreads) pr_persistent(PrArgs a) {
       if (skip) d = a.hub_degree + 1;  // handled by nobody: frozen
       const bool light = vi < a.nodes && !skip && d <= kLight;
       if (light) {
-        // loads issued four at a time so each lane keeps several gathers in
-        // flight; the adds stay in adjacency order
+        // loads issued eight at a time so each lane keeps several gathers in
+        // flight (at most two rounds for 16 neighbours); the adds stay in
+        // adjacency order
         float s = 0.f, c = 0.f;
-        int k = b;
-        for (; k + 4 <= e; k += 4) {
-          const int n0 = __ldg(&a.nlist[k]), n1 = __ldg(&a.nlist[k + 1]);
-          const int n2 = __ldg(&a.nlist[k + 2]), n3 = __ldg(&a.nlist[k + 3]);
-          const float x0 = cur[n0], x1 = cur[n1], x2 = cur[n2], x3 = cur[n3];
-          kahan_add(s, c, x0);
-          kahan_add(s, c, x1);
-          kahan_add(s, c, x2);
-          kahan_add(s, c, x3);
-        }
-        if (k < e) {
-          const int r = e - k;  // 1..3 left
-          const int n0 = __ldg(&a.nlist[k]);
-          const int n1 = r > 1 ? __ldg(&a.nlist[k + 1]) : n0;
-          const int n2 = r > 2 ? __ldg(&a.nlist[k + 2]) : n0;
-          const float x0 = cur[n0], x1 = cur[n1], x2 = cur[n2];
-          kahan_add(s, c, x0);
-          if (r > 1) kahan_add(s, c, x1);
-          if (r > 2) kahan_add(s, c, x2);
+        for (int k = b; k < e; k += 8) {
+          int nb[8];
+#pragma unroll
+          for (int t = 0; t < 8; t++) nb[t] = k + t < e ? __ldg(&a.nlist[k + t]) : -1;
+          float x[8];
+#pragma unroll
+          for (int t = 0; t < 8; t++) x[t] = nb[t] >= 0 ? cur[nb[t]] : 0.f;
+#pragma unroll
+          for (int t = 0; t < 8; t++)
+            if (nb[t] >= 0) kahan_add(s, c, x[t]);
         }
         sum = __fsub_rn(s, c);
       }
@@ -398,8 +390,19 @@ __global__ void __launch_bounds__(kThreads) pr_persistent(PrArgs a) {
     double* slot = a.blkerr + (it & 1) * G;
     if (threadIdx.x == 0) slot[blockIdx.x] = berr;
     if (!grid_sync(ctl, a.timeout_ns)) return;
-    residual = 0;
-    for (int b = 0; b < G; b++) residual += ld_relaxed(&slot[b]);
+    // the grid's residual: warp 0 of every block sums the block partials with
+    // the same fixed tree (lane-strided sums, then a shuffle tree), so every
+    // block reaches the same value and the same stop decision
+    __shared__ double s_res;
+    if (threadIdx.x < 32) {
+      double r = 0.0;
+      for (int b = threadIdx.x; b < G; b += 32) r += ld_relaxed(&slot[b]);
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) r += __shfl_xor_sync(IG_FULL, r, o);
+      if (threadIdx.x == 0) s_res = r;
+    }
+    __syncthreads();
+    residual = s_res;
     float* t = cur;
     cur = nxt;
     nxt = t;
