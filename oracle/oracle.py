@@ -41,6 +41,12 @@ def build_ref(reference_root: str | None = None) -> bool:
     return ref_available()
 
 
+def reference_tree_present(reference_root: str | None = None) -> bool:
+    """Whether the reference sources are on this machine (build_ref can run)."""
+    root = reference_root or os.environ.get("INDIGO_REFERENCE", "/root/reference")
+    return os.path.isdir(os.path.join(root, "include"))
+
+
 def ref_available() -> bool:
     return all(os.access(REF_DIR / f"ref_{a}", os.X_OK) for a in ("bfs", "sssp", "cc", "mis", "pr", "tc"))
 

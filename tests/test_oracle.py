@@ -106,7 +106,12 @@ def test_pr_f64_converges(ig, orc):
     assert res < 1e-13 and it < 2000
 
 
-@pytest.mark.skipif(not os.path.isdir("/root/reference/include"), reason="reference tree not present")
+def _reference_tree() -> bool:
+    from oracle import oracle
+    return oracle.reference_tree_present()
+
+
+@pytest.mark.skipif(not _reference_tree(), reason="reference tree not present")
 def test_oracle_against_live_reference_programs(ig, orc):
     assert orc.build_ref()
     g = ig.rmat(11, 16, seed=21, maxw=1000)
