@@ -24,6 +24,7 @@ struct Captured {
   cudaGraphExec_t exec = nullptr;
   long long kernels = 0;  // kernels launched by one replay
   const void* key[3] = {nullptr, nullptr, nullptr};
+  unsigned long long generation = 0;  // scratch generation the graph was captured with
   float f = 0.f;
   int i = 0;
 };
@@ -129,7 +130,11 @@ static int batch_run(ig_batch* b, int algo, const void* k0, const void* k1, floa
   b->ex.opts = b->tuned[algo] ? &b->opts[algo] : nullptr;
   int rc;
   Captured& c = b->cap[algo];
-  const bool same = c.exec && c.key[0] == k0 && c.key[1] == k1 && c.f == f && c.i == i;
+  // a captured graph holds scratch addresses: reuse it only with the same
+  // arguments and while no scratch slot has been reallocated since (another
+  // algorithm's first run may grow a slot this one uses)
+  const bool same = c.exec && c.key[0] == k0 && c.key[1] == k1 && c.f == f && c.i == i &&
+                    c.generation == b->scratch.generation;
   if (b->use_graphs && (same || b->warm[algo] > 0)) {
     if (!same) {
       if (c.exec) {
@@ -158,6 +163,7 @@ static int batch_run(ig_batch* b, int algo, const void* k0, const void* k1, floa
       c.key[1] = k1;
       c.f = f;
       c.i = i;
+      c.generation = b->scratch.generation;
     }
     rc = batch_cuda(cudaGraphLaunch(c.exec, b->stream), "graph launch");
     if (rc == IG_OK) ig_count_launches((int)c.kernels);

@@ -69,6 +69,9 @@ struct IgScratch {
   void* ptr[IG_SLOT_COUNT] = {};
   size_t cap[IG_SLOT_COUNT] = {};
   int device = -1;
+  // bumped whenever a slot is reallocated: launches captured into a CUDA
+  // graph hold slot addresses and must be captured again after a change
+  unsigned long long generation = 0;
 };
 
 int ig_scratch_get(IgScratch* s, int slot, size_t bytes, void** out);

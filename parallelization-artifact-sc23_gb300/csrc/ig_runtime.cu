@@ -55,7 +55,12 @@ int ig_scratch_get(IgScratch* s, int slot, size_t bytes, void** out) {
   if (slot < 0 || slot >= IG_SLOT_COUNT) return ig_fail(IG_ERR_INVALID_ARG, "bad scratch slot");
   bytes = std::max<size_t>(bytes, 256);
   if (s->cap[slot] < bytes) {
-    if (s->ptr[slot]) cudaFree(s->ptr[slot]);
+    if (s->ptr[slot]) {
+      // work already queued on a stream may still use the old block
+      IG_CU(cudaDeviceSynchronize());
+      cudaFree(s->ptr[slot]);
+    }
+    s->generation++;
     s->ptr[slot] = nullptr;
     s->cap[slot] = 0;
     const size_t want = bytes + bytes / 8;  // headroom for slightly larger graphs
@@ -69,6 +74,7 @@ int ig_scratch_get(IgScratch* s, int slot, size_t bytes, void** out) {
 }
 
 void ig_scratch_release(IgScratch* s) {
+  s->generation++;
   for (int i = 0; i < IG_SLOT_COUNT; i++) {
     if (s->ptr[i]) cudaFree(s->ptr[i]);
     s->ptr[i] = nullptr;

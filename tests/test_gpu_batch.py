@@ -131,3 +131,28 @@ def test_autotune_keeps_results(ig, gpu, expected):
             assert np.array_equal(lab[v0:v1], e_lab), (call, i, "cc")
             assert int(cnt[i]) == e_tc, (call, i, "tc")
             assert int(its[i]) == e_it and np.array_equal(sc[v0:v1], e_sc), (call, i, "pr")
+
+
+def test_captures_follow_scratch_growth(ig, gpu, expected):
+    """BFS and CC are captured into CUDA graphs before the first TC call,
+    whose larger buffers make the batch's shared scratch slots grow; the next
+    BFS and CC calls must be captured again (their graphs held the old
+    addresses) and give the same results."""
+    u, vptr = ig.gen_batch(48, vmin=64, vmax=4096, seed=13, maxw=255)
+    with ig.Batch(u, vptr) as b:
+        V = b.nodes
+        dist, lab, cnt = ig.DeviceBuffer(4 * V), ig.DeviceBuffer(4 * V), ig.DeviceBuffer(8 * b.graphs)
+        for _ in range(2):  # direct, then captured
+            b.bfs(dist)
+            b.cc(lab)
+        b.tc(cnt)  # first TC call: grows scratch slots BFS and CC use
+        for _ in range(2):  # captured again, then replayed
+            b.bfs(dist)
+            b.cc(lab)
+            assert b.last_run().status == 0
+            d, l = dist.to_array(np.int32, V), lab.to_array(np.int32, V)
+            for i, (e_dist, e_lab, e_tc, _, _) in enumerate(expected):
+                v0, v1 = b.vptr[i], b.vptr[i + 1]
+                assert np.array_equal(d[v0:v1], e_dist) and np.array_equal(l[v0:v1], e_lab), i
+        c = cnt.to_array(np.uint64, b.graphs)
+        assert all(int(c[i]) == e[2] for i, e in enumerate(expected))
