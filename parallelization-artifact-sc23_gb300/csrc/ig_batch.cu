@@ -182,7 +182,7 @@ static int bfs_body(ig_batch* b, IgExec* ex, const int* src, int* d_dist) {
   return igk_bfs_multi(ex, &b->g, src, b->graphs, d_dist);
 }
 static int cc_body(ig_batch* b, IgExec* ex, int* d_label) {
-  int rc = igk_cc(ex, &b->g, d_label);
+  int rc = igk_cc(ex, &b->g, d_label, false);  // many small components: no giant one to skip
   if (rc) return rc;
   return igk_cc_localize(ex, d_label, b->vptr, b->graphs);
 }

@@ -23,8 +23,9 @@
 //   compress: parent[v] = root(v)
 //   giant   : the most frequent root among a fixed sample of vertices
 //   hook    : vertices whose root is not the giant one: union(v, w) for their
-//             neighbours from position kSample on; vertices above the hub
-//             degree are deferred to an edge-balanced grid-wide pass
+//             neighbours from position kSample on (only w < v when there is
+//             no giant component); vertices above the hub degree are
+//             deferred to an edge-balanced grid-wide pass
 //   compress: label[v] = root(v)
 #include "ig_device.cuh"
 #include "ig_options.h"
@@ -90,7 +91,10 @@ __global__ void cc_sample(const int* __restrict__ nindex, const int* __restrict_
 }
 
 // The most frequent root among kGiantSamples evenly spaced vertices (parent
-// is compressed, so parent[x] is x's root); one block.  Written to ctl->i32[1].
+// is compressed, so parent[x] is x's root); one block.  Written to ctl->i32[1],
+// or -1 when it covers less than 1/8 of the samples (no giant component, as in
+// a union of many small graphs): then no vertex is skipped and every
+// undirected edge is linked once, from its larger end.
 __global__ void __launch_bounds__(kThreads) cc_giant(const int* parent, int n, IgCtl* ctl) {
   __shared__ int s_root[kGiantSamples];
   __shared__ unsigned long long s_best;
@@ -105,23 +109,28 @@ __global__ void __launch_bounds__(kThreads) cc_giant(const int* parent, int n, I
     atomicMax(&s_best, ((unsigned long long)c << 32) | (unsigned)(0x7fffffff - s_root[i]));
   }
   __syncthreads();
-  if (threadIdx.x == 0) ctl->i32[1] = 0x7fffffff - (int)(s_best & 0xffffffffu);
+  if (threadIdx.x == 0) {
+    const int count = (int)(s_best >> 32);
+    ctl->i32[1] = count * 8 >= m ? 0x7fffffff - (int)(s_best & 0xffffffffu) : -1;
+  }
 }
 
 __global__ void __launch_bounds__(kThreads) cc_hook(const int* __restrict__ nindex, const int* __restrict__ nlist,
-                                                    int n, int* parent, int* hubs, IgCtl* ctl, int hub_degree) {
+                                                    int n, int* parent, int* hubs, IgCtl* ctl, int hub_degree,
+                                                    int first) {
   using namespace ig;
   const int lane = lane_id();
   const long long gtid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   const long long gthreads = (long long)gridDim.x * blockDim.x;
   const int giant = ctl->i32[1];
+  const bool half = giant < 0;  // no giant component: each edge once, from its larger end
   for (long long base = gtid & ~31LL; base < n; base += gthreads) {
     const long long v = base + lane;
     int beg = 0, deg = 0;
     // a vertex still pointing at the giant root is in the giant component:
     // its edges to other components are linked from their other ends
     if (v < n && load_parent(parent, (int)v) != giant) {
-      beg = __ldg(&nindex[v]) + kSample;
+      beg = __ldg(&nindex[v]) + first;  // positions below `first` were linked by the sampling
       deg = max(0, __ldg(&nindex[v + 1]) - beg);
     }
     const bool hub = deg > hub_degree;
@@ -129,7 +138,10 @@ __global__ void __launch_bounds__(kThreads) cc_hook(const int* __restrict__ nind
     const int vv = (int)v;
     warp_expand(beg, hub ? 0 : deg, [&](bool act, int e, int j) {
       const int u = __shfl_sync(IG_FULL, vv, j);
-      if (act) unite(parent, u, __ldg(&nlist[e]));
+      if (act) {
+        const int w = __ldg(&nlist[e]);
+        if (!half || w < u) unite(parent, u, w);
+      }
     });
   }
 }
@@ -140,8 +152,12 @@ __global__ void __launch_bounds__(kThreads) cc_hook_hubs(const int* __restrict__
   using namespace ig;
   const int nh = ctl->i32[0];
   if (nh == 0) return;
+  const bool half = ctl->i32[1] < 0;
   grid_expand_hubs(nindex, hubs, nh, [&](bool act, int e, int hv) {
-    if (act) unite(parent, hv, __ldg(&nlist[e]));
+    if (act) {
+      const int w = __ldg(&nlist[e]);
+      if (!half || w < hv) unite(parent, hv, w);
+    }
   });
 }
 
@@ -174,7 +190,7 @@ int igk_cc_localize(IgExec* ex, int* d_label, const int* d_graph_vptr, int graph
   return ig_cuda_check((int)cudaGetLastError(), "cc localize launch");
 }
 
-int igk_cc(IgExec* ex, const ig_csr* dg, int* d_label) {
+int igk_cc(IgExec* ex, const ig_csr* dg, int* d_label, bool sample) {
   const int n = dg->nodes;
   void* hubs;
   int rc;
@@ -184,13 +200,19 @@ int igk_cc(IgExec* ex, const ig_csr* dg, int* d_label) {
   const int grid_v = std::min((n + kThreads - 1) / kThreads, ex->sms * 16);
   const int grid_w = std::max(1, std::min((n + kThreads - 1) / kThreads, ex->sms * 8));
   cc_init<<<grid_v, kThreads, 0, ex->stream>>>(dg->nindex, dg->nlist, n, d_label);
-  cc_sample<<<grid_v, kThreads, 0, ex->stream>>>(dg->nindex, dg->nlist, n, d_label);
-  cc_compress<<<grid_v, kThreads, 0, ex->stream>>>(d_label, n);
-  cc_giant<<<1, kThreads, 0, ex->stream>>>(d_label, n, ex->d_ctl);
+  if (sample) {
+    cc_sample<<<grid_v, kThreads, 0, ex->stream>>>(dg->nindex, dg->nlist, n, d_label);
+    cc_compress<<<grid_v, kThreads, 0, ex->stream>>>(d_label, n);
+    cc_giant<<<1, kThreads, 0, ex->stream>>>(d_label, n, ex->d_ctl);
+    ig_count_launches(3);
+  } else if ((rc = ig_cuda_check((int)cudaMemsetAsync(&ex->d_ctl->i32[1], 0xff, sizeof(int), ex->stream),
+                                 "memset"))) {
+    return rc;  // i32[1] = -1: no giant component, every edge linked once from its larger end
+  }
   cc_hook<<<grid_w, kThreads, 0, ex->stream>>>(dg->nindex, dg->nlist, n, d_label, (int*)hubs, ex->d_ctl,
-                                               o.hub_degree);
+                                               o.hub_degree, sample ? kSample : 0);
   cc_hook_hubs<<<ex->sms * 4, kThreads, 0, ex->stream>>>(dg->nindex, dg->nlist, d_label, (int*)hubs, ex->d_ctl);
   cc_compress<<<grid_v, kThreads, 0, ex->stream>>>(d_label, n);
-  ig_count_launches(7);
+  ig_count_launches(4);
   return ig_cuda_check((int)cudaGetLastError(), "cc launch");
 }

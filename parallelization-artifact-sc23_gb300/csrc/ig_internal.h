@@ -132,7 +132,9 @@ void ig_count_launches(int n);
 int igk_bfs(IgExec* ex, const ig_csr* dg, int src, int* d_dist);
 int igk_bfs_launch_prealloc(IgExec* ex, const ig_csr* dg, int src, int* d_dist, int* qa, int* qb, int* hubs);
 int igk_sssp(IgExec* ex, const ig_csr* dg, int src, int* d_dist);
-int igk_cc(IgExec* ex, const ig_csr* dg, int* d_label);
+// sample: link the first neighbours and skip the largest component's vertices
+// (skewed single graphs); off for unions of many small graphs
+int igk_cc(IgExec* ex, const ig_csr* dg, int* d_label, bool sample = true);
 int igk_mis(IgExec* ex, const ig_csr* dg, int* d_status, unsigned int* d_prio);
 int igk_pr(IgExec* ex, const ig_csr* dg, const int* d_degree, float* d_scores,
            float epsilon, int max_iter);
