@@ -59,18 +59,8 @@ struct PrArgs {
   int graphs;
   double* gres;
   int* giters;
+  int* vgraph;  // graph of every vertex (filled by the kernel before the first iteration)
 };
-
-// graph of vertex v: largest g with graph_vptr[g] <= v
-__device__ __forceinline__ int graph_of(const PrArgs& a, int v) {
-  int lo = 0, hi = a.graphs - 1;
-  while (lo < hi) {
-    const int mid = (lo + hi + 1) >> 1;
-    if (__ldg(&a.graph_vptr[mid]) <= v) lo = mid;
-    else hi = mid - 1;
-  }
-  return lo;
-}
 
 // Adds each lane's x into gres[g_lane] with one atomic per distinct graph of the warp.
 __device__ __forceinline__ void warp_add_by_graph(double* gres, int g, double x, bool valid) {
@@ -199,6 +189,10 @@ __global__ void __launch_bounds__(kThreads) pr_persistent(PrArgs a) {
   // ---- initial contributions, hub census per contiguous block range
   for (long long v = gtid; v < a.nodes; v += gthreads)
     a.ca[v] = __fdiv_rn(a.scores[v], (float)vdegree(a, (int)v));
+  if (kBatched)  // vertex -> graph, one block per graph (read after the next barrier)
+    for (int g = blockIdx.x; g < a.graphs; g += G)
+      for (int v = __ldg(&a.graph_vptr[g]) + threadIdx.x; v < __ldg(&a.graph_vptr[g + 1]); v += blockDim.x)
+        a.vgraph[v] = g;
   const long long r0 = (long long)a.nodes * blockIdx.x / G, r1 = (long long)a.nodes * (blockIdx.x + 1) / G;
   {
     int nh = 0, nc = 0;
@@ -280,7 +274,7 @@ __global__ void __launch_bounds__(kThreads) pr_persistent(PrArgs a) {
     for (int c = warp_g; c < nchunks; c += nwarps) {
       const int lo = a.chunk_hub[c];  // owning hub
       const int hv = a.hubs[lo];
-      if (kBatched && frozen(graph_of(a, hv))) continue;
+      if (kBatched && frozen(a.vgraph[hv])) continue;
       const int hb = __ldg(&a.nindex[hv]), he = __ldg(&a.nindex[hv + 1]);
       const int b = hb + (c - a.chunk_base[lo]) * a.chunk;
       const int e = min(b + a.chunk, he);
@@ -301,7 +295,7 @@ __global__ void __launch_bounds__(kThreads) pr_persistent(PrArgs a) {
       float vbase = a.base;
       bool skip = false;
       if (kBatched && vi < a.nodes) {
-        vg = graph_of(a, v);
+        vg = a.vgraph[v];
         skip = frozen(vg);
         vbase = __fdiv_rn(__fsub_rn(1.0f, a.damp),
                           (float)(__ldg(&a.graph_vptr[vg + 1]) - __ldg(&a.graph_vptr[vg])));
@@ -369,7 +363,7 @@ __global__ void __launch_bounds__(kThreads) pr_persistent(PrArgs a) {
         int hg = 0;
         float hbase = a.base;
         if (kBatched) {
-          hg = graph_of(a, v);
+          hg = a.vgraph[v];
           if (frozen(hg)) continue;
           hbase = __fdiv_rn(__fsub_rn(1.0f, a.damp),
                             (float)(__ldg(&a.graph_vptr[hg + 1]) - __ldg(&a.graph_vptr[hg])));
@@ -444,7 +438,7 @@ static int pr_launch(IgExec* ex, const ig_csr* dg, const int* d_degree, float* d
   const long long max_hubs = (long long)dg->edges / (hub_degree + 1) + 1;
   const long long max_chunks = (long long)dg->edges / chunk + max_hubs + 1;
   const int max_blocks = ex->sms * 32;
-  void *ca, *cb, *hubs, *cbase, *chub, *part, *blk, *blkerr, *gres = nullptr;
+  void *ca, *cb, *hubs, *cbase, *chub, *part, *blk, *blkerr, *gres = nullptr, *vgraph = nullptr;
   int rc;
   if ((rc = ig_scratch_get(ex->scratch, IG_SLOT_F0, (size_t)n * sizeof(float), &ca))) return rc;
   if ((rc = ig_scratch_get(ex->scratch, IG_SLOT_F1, (size_t)n * sizeof(float), &cb))) return rc;
@@ -456,6 +450,7 @@ static int pr_launch(IgExec* ex, const ig_csr* dg, const int* d_degree, float* d
   if ((rc = ig_scratch_get(ex->scratch, IG_SLOT_BLK, (size_t)2 * max_blocks * sizeof(double), &blkerr))) return rc;
   if (d_graph_vptr) {
     if ((rc = ig_scratch_get(ex->scratch, IG_SLOT_V1, (size_t)3 * graphs * sizeof(double), &gres))) return rc;
+    if ((rc = ig_scratch_get(ex->scratch, IG_SLOT_G2, (size_t)n * sizeof(int), &vgraph))) return rc;
     if ((rc = ig_cuda_check((int)cudaMemsetAsync(gres, 0, (size_t)3 * graphs * sizeof(double), ex->stream), "memset")))
       return rc;
     if ((rc = ig_cuda_check((int)cudaMemsetAsync(d_iters, 0, (size_t)graphs * sizeof(int), ex->stream), "memset")))
@@ -466,7 +461,7 @@ static int pr_launch(IgExec* ex, const ig_csr* dg, const int* d_degree, float* d
   const float base = (1.0f - damp) / (float)n;
   PrArgs a{dg->nindex, dg->nlist, d_degree, n, dg->edges, d_scores, (float*)ca, (float*)cb, (int*)hubs,
            (int*)cbase, (int*)chub, (float2*)part, (int*)blk, (double*)blkerr, ex->d_ctl, epsilon, max_iter, base, damp,
-           ex->timeout_ns, hub_degree, chunk, d_graph_vptr, graphs, (double*)gres, d_iters};
+           ex->timeout_ns, hub_degree, chunk, d_graph_vptr, graphs, (double*)gres, d_iters, (int*)vgraph};
   void* args[] = {&a};
   const int bps = o.pr_blocks_per_sm > 0 ? o.pr_blocks_per_sm : o.blocks_per_sm;
   const int cap = bps > 0 ? std::min(bps, 32) : 32;
