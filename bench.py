@@ -625,6 +625,8 @@ def run_batched(args, dist: Dist):
     launches = ig.kernel_launches() - launches0
     if b.last_run().status:
         raise RuntimeError("batched run failed during timing")
+    its = d_its.to_array(np.int32, graphs_here)
+    pr_its = {"min": int(its.min()), "median": float(np.median(its)), "max": int(its.max())}
     ms = dist.max(t_a.elapsed_ms(t_b)) / args.steps
     graphs_all = int(dist.sum(graphs_here))
     value = graphs_all / (ms * 1e-3)
@@ -659,6 +661,7 @@ def run_batched(args, dist: Dist):
                        "vmin": BATCH_VMIN, "vmax": BATCH_VMAX, "seed": BATCH_SEED,
                        "l2": "inputs larger than L2 (%.0f MB neighbour lists)" % (4 * u.edges / 1e6)},
             "per_algo_ms": {k: round(v / args.steps, 3) for k, v in acc.items()},
+            "pr_iterations_per_graph": pr_its,
             "autotuned": tuned,
             "plain": {"value": round(plain_value, 1), "unit": "graphs/s", "sample_graphs": int(len(sample)),
                       "api": "drop-in C ABI, one call per graph and algorithm (host wall clock, results to host)"},
