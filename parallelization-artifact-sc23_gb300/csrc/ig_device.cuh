@@ -415,66 +415,6 @@ __device__ __forceinline__ void warp_expand4(int beg, int deg, Visit4&& visit4) 
 
 namespace ig {
 
-// Edge-balanced expansion of the hubs' adjacency lists over the whole grid,
-// four 32-edge slots per lane per step.  Each warp takes windows of 128
-// consecutive edges of the hubs' concatenated lists (so its loads are
-// coalesced and its slots mostly share one hub): one warp-uniform binary
-// search finds the window's first hub, and each slot walks forward from it
-// (at most one step while hubs have more than 128 edges).  aux(v) is read once
-// per hub when the batch is staged (e.g. the hub's distance).
-// visit4(act[4], edge[4], hub_vertex[4], aux[4]) is called warp-uniformly.
-// Requires blockDim.x * 4 >= kHubBatch and all threads of every block.
-template <class Aux, class Visit4>
-__device__ __forceinline__ void grid_expand_hubs4(const int* __restrict__ nindex, const int* hubs, int nh,
-                                                  Aux&& aux, Visit4&& visit4) {
-  __shared__ long long s_pref[kHubBatch + 1];
-  __shared__ int s_beg[kHubBatch];
-  __shared__ int s_v[kHubBatch];
-  __shared__ int s_aux[kHubBatch];
-  __shared__ long long s_warp[32];
-  const int lane = lane_id();
-  const long long gwarp = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  const long long nwarps = ((long long)gridDim.x * blockDim.x) >> 5;
-  for (int hb = 0; hb < nh; hb += kHubBatch) {
-    const int cnt = min(kHubBatch, nh - hb);
-    __syncthreads();
-    for (int i = threadIdx.x; i < cnt; i += blockDim.x) {
-      const int v = hubs[hb + i];
-      const int b = __ldg(&nindex[v]);
-      s_v[i] = v;
-      s_beg[i] = b;
-      s_pref[i] = __ldg(&nindex[v + 1]) - b;
-      s_aux[i] = aux(v);
-    }
-    __syncthreads();
-    block_exclusive_scan64(s_pref, cnt, s_warp);
-    const long long total = s_pref[cnt];
-    for (long long base = gwarp * 128; base < total; base += nwarps * 128) {
-      int j0 = 0, span = cnt;  // largest j with s_pref[j] <= base
-      while (span > 1) {
-        const int half = span >> 1;
-        if (s_pref[j0 + half] <= base) j0 += half;
-        span -= half;
-      }
-      bool act[4];
-      int edge[4], hv[4], ha[4];
-#pragma unroll
-      for (int k = 0; k < 4; k++) {
-        const long long e = base + k * 32 + lane;
-        act[k] = e < total;
-        int j = j0;
-        if (act[k])
-          while (s_pref[j + 1] <= e) j++;
-        edge[k] = act[k] ? s_beg[j] + (int)(e - s_pref[j]) : 0;
-        hv[k] = s_v[j];
-        ha[k] = s_aux[j];
-      }
-      visit4(act, edge, hv, ha);
-    }
-  }
-  __syncthreads();
-}
-
 }  // namespace ig
 
 

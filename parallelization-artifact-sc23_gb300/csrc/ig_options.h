@@ -9,8 +9,8 @@ struct IgOptions {
   long long sssp_delta;   // near/far bucket width (0 = derived from sampled weights)
   int sssp_delta_scale;   // derived width = mean weight * scale / mean degree
   int sssp_heavy_split;   // 1: heavy edges (w >= delta) relaxed once per bucket
-  int sssp_hub_degree;    // SSSP: degree above which a vertex is expanded by the whole grid
-  int sssp_warp_degree;   // SSSP: degree above which a vertex is expanded by a whole warp
+  int sssp_item_edges;    // SSSP: edges per work item of a list longer than sssp_warp_degree
+  int sssp_warp_degree;   // SSSP: lists longer than this become work items expanded one warp each
   int pr_hub_degree;      // PageRank: degree above which a vertex is split in chunks
   int pr_chunk;           // PageRank: edges per hub chunk
   int pr_blocks_per_sm;   // PageRank: resident blocks per SM (0 = blocks_per_sm)

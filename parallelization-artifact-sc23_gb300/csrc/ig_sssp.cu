@@ -10,8 +10,11 @@
 // Output semantics follow include/sssp_vertex_cuda.h: shortest distance,
 // INT_MAX if unreachable (checked there against CPUserialDijkstra, :74-99).
 //
-// Near phase: the near queue is expanded 32 vertices per warp (hubs by the
-// whole grid); an improved vertex with distance < T joins the next near queue
+// Near phase: the near queue is expanded in chunks of 32 vertices per warp;
+// a vertex with more than warp_degree neighbours instead becomes work items of
+// item_edges edges, expanded after the round's barrier one whole warp per item
+// and taken dynamically, so no warp holds the round up with a long list.  An
+// improved vertex with distance < T joins the next near queue
 // (once per iteration, by stamp) and otherwise the far pile (once per epoch,
 // by flag).  A queued vertex is expanded only if its distance is below the
 // one it was last expanded with (re-queued vertices are often expanded
@@ -41,15 +44,16 @@ struct SsspArgs {
   int* fb;
   int* stamp;    // near-queue membership stamp
   int* farflag;  // far-pile membership (epoch + 1)
-  int* hubs;
-  int* mlist;     // per-round list of medium vertices (expanded one per warp)
+  int* mlist;     // per-round list of work items: vertex ...
+  int* mchunk;    // ... and which `item_edges`-edge chunk of its list
+  int mcap;       // item capacity
   int* expanded;  // distance each vertex was last expanded with (INT_MAX: never)
   int* members;   // vertices light-expanded since the last heavy pass
   int* inmember;  // 1 while a vertex sits in members
   IgCtl* ctl;
   unsigned long long timeout_ns;
-  int hub_degree;
-  int warp_degree;       // vertices with more neighbours than this (up to hub_degree) go to mlist
+  int item_edges;        // edges per work item
+  int warp_degree;       // vertices with more neighbours than this go to mlist as work items
   long long delta;       // > 0: fixed bucket width
   int delta_scale;
   int heavy_split;       // 1: light/heavy edge split (heavy edges relaxed once per bucket)
@@ -134,7 +138,6 @@ __global__ void __launch_bounds__(kThreads, 4) sssp_persistent(SsspArgs a) {
         if (heavy) ctl->i32[9 + (mpass + 1) % 2] = 0;
       }
       int* qsize = &ctl->i32[(it + 1) % 3];
-      int* nhub = &ctl->i32[3 + it % 3];
       int* nmembers = &ctl->i32[9 + mpass % 2];
       int* far = (epoch & 1) ? a.fb : a.fa;
       int* fsize = &ctl->i32[6 + epoch % 3];
@@ -208,16 +211,38 @@ __global__ void __launch_bounds__(kThreads, 4) sssp_persistent(SsspArgs a) {
         }
         if (a.heavy_split && !heavy)
           warp_append(expand && atomicExch(&a.inmember[u], 1) == 0, u, a.members, nmembers, a.nodes, ctl);
-        const bool hub = deg > a.hub_degree;
-        const bool medium = !hub && deg > a.warp_degree;
-        warp_append(hub, u, a.hubs, nhub, a.nodes, ctl);
-        warp_append(medium, u, a.mlist, &ctl->i32[15 + it % 3], a.nodes, ctl);
+        // a list longer than warp_degree becomes work items of item_edges
+        // edges each, expanded after the barrier one warp per item
+        const bool listed = deg > a.warp_degree;
+        {
+          const int cnt = listed ? (deg + a.item_edges - 1) / a.item_edges : 0;
+          int incl = cnt;
+#pragma unroll
+          for (int o = 1; o < 32; o <<= 1) {
+            const int t = __shfl_up_sync(IG_FULL, incl, o);
+            if (lane >= o) incl += t;
+          }
+          const int total = __shfl_sync(IG_FULL, incl, 31);
+          if (total > 0) {
+            int ibase = 0;
+            if (lane == 31) ibase = atomicAdd(&ctl->i32[15 + it % 3], total);
+            ibase = __shfl_sync(IG_FULL, ibase, 31) + incl - cnt;
+            for (int c = 0; c < cnt; c++) {
+              if (ibase + c < a.mcap) {
+                a.mlist[ibase + c] = u;
+                a.mchunk[ibase + c] = c;
+              } else {
+                raise(ctl, IG_ERR_OVERFLOW);
+              }
+            }
+          }
+        }
         if (expand) {
           frontier_v++;
           frontier_e += deg;
         }
         // the chunk's short lists here: at most 32 * warp_degree edges per warp
-        warp_expand4(beg, (hub || medium) ? 0 : deg, [&](const bool (&act)[4], const int (&e)[4], const int (&j)[4]) {
+        warp_expand4(beg, listed ? 0 : deg, [&](const bool (&act)[4], const int (&e)[4], const int (&j)[4]) {
           int duj[4];
 #pragma unroll
           for (int k = 0; k < 4; k++) duj[k] = __shfl_sync(IG_FULL, du, j[k]);
@@ -230,26 +255,20 @@ __global__ void __launch_bounds__(kThreads, 4) sssp_persistent(SsspArgs a) {
       warp_buf_flush(nbuf, nbuf_n, nxt, qsize, a.nodes, ctl);
       warp_buf_flush(fbuf, fbuf_n, far, fsize, a.nodes, ctl);
       if (!grid_sync(ctl, a.timeout_ns)) return;
-      const int nh = ld_relaxed(nhub);
       const int nm = ld_relaxed(&ctl->i32[15 + it % 3]);
-      if (nh > 0 || nm > 0) {
-        // hub distances are read once per staged hub; a hub improved since
-        // was queued again and is expanded with its new distance next round
-        if (nh > 0)
-          grid_expand_hubs4(a.nindex, a.hubs, nh, [&](int v) { return a.dist[v]; },
-                            [&](const bool (&act)[4], const int (&e)[4], const int (&)[4], const int (&du)[4]) {
-                              relax4(act, e, du);
-                            });
-        // medium vertices, one whole warp each over its contiguous list (no
-        // owner search), four at a time taken from a counter after the first
-        // four by warp index, so warps that finished their hub share early
-        // take more
+      if (nm > 0) {
+        // work items (vertex, chunk of item_edges edges), one whole warp each
+        // over a contiguous range (no owner search), four at a time taken
+        // from a counter after the first four by warp index; the vertex's
+        // distance is read when its item starts
         int* mgrab = &ctl->i32[18 + it % 3];
         for (int m0 = warp_g * 4; m0 < nm;) {
           for (int mi = m0; mi < min(m0 + 4, nm); mi++) {
             const int u = a.mlist[mi];
             const int du = a.dist[u];
-            const int b = __ldg(&a.nindex[u]), d = __ldg(&a.nindex[u + 1]) - b;
+            const int b0 = __ldg(&a.nindex[u]), d0 = __ldg(&a.nindex[u + 1]) - b0;
+            const int off0 = a.mchunk[mi] * a.item_edges;
+            const int b = b0 + off0, d = min(a.item_edges, d0 - off0);
             for (int base = 0; base < d; base += 128) {
               bool act[4];
               int e[4], duk[4];
@@ -344,7 +363,7 @@ __global__ void __launch_bounds__(kThreads, 4) sssp_persistent(SsspArgs a) {
 
 int igk_sssp(IgExec* ex, const ig_csr* dg, int src, int* d_dist) {
   const size_t vb = (size_t)dg->nodes * sizeof(int);
-  void *qa, *qb, *fa, *fb, *stamp, *farflag, *hubs, *mlist;
+  void *qa, *qb, *fa, *fb, *stamp, *farflag, *mlist, *mchunk;
   int rc;
   if ((rc = ig_scratch_get(ex->scratch, IG_SLOT_Q0, vb, &qa))) return rc;
   if ((rc = ig_scratch_get(ex->scratch, IG_SLOT_Q1, vb, &qb))) return rc;
@@ -352,8 +371,12 @@ int igk_sssp(IgExec* ex, const ig_csr* dg, int src, int* d_dist) {
   if ((rc = ig_scratch_get(ex->scratch, IG_SLOT_Q3, vb, &fb))) return rc;
   if ((rc = ig_scratch_get(ex->scratch, IG_SLOT_V0, vb, &stamp))) return rc;
   if ((rc = ig_scratch_get(ex->scratch, IG_SLOT_V1, vb, &farflag))) return rc;
-  if ((rc = ig_scratch_get(ex->scratch, IG_SLOT_V2, vb, &hubs))) return rc;
-  if ((rc = ig_scratch_get(ex->scratch, IG_SLOT_G0, vb, &mlist))) return rc;
+  // items: sum over a round's vertices of ceil(deg / item edges) <= nodes + edges / item edges
+  const IgOptions& op = ig_exec_options(ex);
+  const long long mcap_l = (long long)dg->nodes + dg->edges / std::max(1, op.sssp_item_edges) + 1;
+  const int mcap = (int)std::min<long long>(mcap_l, 0x7fffffffLL);
+  if ((rc = ig_scratch_get(ex->scratch, IG_SLOT_G0, (size_t)mcap * sizeof(int), &mlist))) return rc;
+  if ((rc = ig_scratch_get(ex->scratch, IG_SLOT_G1, (size_t)mcap * sizeof(int), &mchunk))) return rc;
   void *expanded, *members, *inmember;
   if ((rc = ig_scratch_get(ex->scratch, IG_SLOT_F0, vb, &expanded))) return rc;
   if ((rc = ig_scratch_get(ex->scratch, IG_SLOT_F1, vb, &members))) return rc;
@@ -361,8 +384,9 @@ int igk_sssp(IgExec* ex, const ig_csr* dg, int src, int* d_dist) {
   if ((rc = ig_exec_reset(ex))) return rc;
   const IgOptions& o = ig_exec_options(ex);
   SsspArgs a{dg->nindex, dg->nlist, dg->eweight, dg->nodes, dg->edges, src, d_dist,
-             (int*)qa, (int*)qb, (int*)fa, (int*)fb, (int*)stamp, (int*)farflag, (int*)hubs, (int*)mlist,
-             (int*)expanded, (int*)members, (int*)inmember, ex->d_ctl, ex->timeout_ns, o.sssp_hub_degree,
+             (int*)qa, (int*)qb, (int*)fa, (int*)fb, (int*)stamp, (int*)farflag, (int*)mlist,
+             (int*)mchunk, mcap,
+             (int*)expanded, (int*)members, (int*)inmember, ex->d_ctl, ex->timeout_ns, o.sssp_item_edges,
              o.sssp_warp_degree,
              o.sssp_delta, o.sssp_delta_scale, o.sssp_heavy_split};
   void* args[] = {&a};
