@@ -144,7 +144,9 @@ int ig_event_elapsed_ms(void* start, void* stop, float* ms);
 /* Bound (milliseconds) on every device-side wait; default 5000. */
 int ig_set_wait_timeout_ms(int ms);
 /* Kernel tuning knobs (process-wide): blocks_per_sm, bfs_alpha, bfs_beta,
- * hub_degree, sssp_delta, sssp_delta_scale, pr_hub_degree, pr_chunk. */
+ * hub_degree, sssp_delta, sssp_delta_scale, sssp_heavy_split,
+ * sssp_item_edges, sssp_warp_degree, sssp_window_scale, sssp_window_degree,
+ * pr_hub_degree, pr_chunk, pr_blocks_per_sm, tc_block_chunk. */
 int ig_set_option(const char* name, long long value);
 int ig_get_option(const char* name, long long* value);
 /* Number of kernels this library has launched in the process. */

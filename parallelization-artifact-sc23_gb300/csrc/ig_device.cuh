@@ -415,11 +415,6 @@ __device__ __forceinline__ void warp_expand4(int beg, int deg, Visit4&& visit4) 
 
 namespace ig {
 
-}  // namespace ig
-
-
-namespace ig {
-
 // Per-warp staging of worklist appends in shared memory.  A warp gathers the
 // items it appends in its own buffer and writes them to the global queue 32
 // at a time (one atomicAdd on the queue counter and one coalesced 128-byte
@@ -480,13 +475,22 @@ __device__ __forceinline__ void warp_buf_drain(int* buf, int& n, int* q, int* qs
   }
 }
 
-// Two warp_buf_append calls for two queues in one: the per-lane counts of
-// both (at most kMax each, so a warp's total fits in 16 bits) are scanned
-// together, and a warp with nothing to append returns after one ballot.
+// Two warp_buf_append calls for two queues in one: slot k of this lane holds
+// v[k], appended to the first queue if f1[k] and to the second if f2[k].  The
+// per-lane counts of both (at most kMax each, so a warp's total fits in 16
+// bits) are scanned together, and a warp with nothing to append returns after
+// one ballot.  Flags rather than compacted arrays keep every register array
+// statically indexed, so nothing goes to local memory.
 template <int kMax>
-__device__ __forceinline__ void warp_buf_append2(int c1, const int (&i1)[kMax], int* b1, int& n1, int* q1, int* s1,
-                                                 int c2, const int (&i2)[kMax], int* b2, int& n2, int* q2, int* s2,
-                                                 int cap, IgCtl* ctl) {
+__device__ __forceinline__ void warp_buf_append2_flags(const int (&v)[kMax], const bool (&f1)[kMax], int* b1, int& n1,
+                                                       int* q1, int* s1, const bool (&f2)[kMax], int* b2, int& n2,
+                                                       int* q2, int* s2, int cap, IgCtl* ctl) {
+  int c1 = 0, c2 = 0;
+#pragma unroll
+  for (int k = 0; k < kMax; k++) {
+    c1 += f1[k];
+    c2 += f2[k];
+  }
   if (__ballot_sync(IG_FULL, (c1 | c2) != 0) == 0) return;
   const int lane = lane_id();
   const int packed = c1 | (c2 << 16);
@@ -498,11 +502,11 @@ __device__ __forceinline__ void warp_buf_append2(int c1, const int (&i1)[kMax], 
   }
   const int total = __shfl_sync(IG_FULL, incl, 31);
   const int ex = incl - packed;
-  const int p1 = n1 + (ex & 0xffff), p2 = n2 + (ex >> 16);
+  int p1 = n1 + (ex & 0xffff), p2 = n2 + (ex >> 16);
 #pragma unroll
   for (int k = 0; k < kMax; k++) {
-    if (k < c1) b1[p1 + k] = i1[k];
-    if (k < c2) b2[p2 + k] = i2[k];
+    if (f1[k]) b1[p1++] = v[k];
+    if (f2[k]) b2[p2++] = v[k];
   }
   n1 += total & 0xffff;
   n2 += total >> 16;

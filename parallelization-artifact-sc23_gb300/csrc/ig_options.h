@@ -11,6 +11,9 @@ struct IgOptions {
   int sssp_heavy_split;   // 1: heavy edges (w >= delta) relaxed once per bucket
   int sssp_item_edges;    // SSSP: edges per work item of a list longer than sssp_warp_degree
   int sssp_warp_degree;   // SSSP: lists longer than this become work items expanded one warp each
+  int sssp_window_scale;  // SSSP: expansion window C = mean weight * scale (0 = off); a queued vertex
+                          // of degree d is expanded once its distance is below round minimum + C / d
+  int sssp_window_degree; // SSSP: vertices of at most this degree are never deferred by the window
   int pr_hub_degree;      // PageRank: degree above which a vertex is split in chunks
   int pr_chunk;           // PageRank: edges per hub chunk
   int pr_blocks_per_sm;   // PageRank: resident blocks per SM (0 = blocks_per_sm)

@@ -18,7 +18,13 @@
 // (once per iteration, by stamp) and otherwise the far pile (once per epoch,
 // by flag).  A queued vertex is expanded only if its distance is below the
 // one it was last expanded with (re-queued vertices are often expanded
-// already).  When the near queue runs dry the far pile is split: the minimum
+// already).  A vertex of degree d above window_degree is expanded only once
+// its distance is below m + C / d (m: the smallest distance queued for the
+// round, C: the window constant) and is otherwise queued again for the next
+// round: a list is expensive to expand with a distance that later improves,
+// so the longer the list, the closer to Dijkstra order it is expanded, while
+// short lists keep the parallelism of expanding everything queued.  When the
+// near queue runs dry the far pile is split: the minimum
 // pending distance m is found, T becomes max(T, m) + delta, entries below the
 // old T are stale (already settled through the near queue) and dropped,
 // entries below the new T form the next near queue, the rest stay far.
@@ -29,6 +35,8 @@ namespace {
 
 constexpr int kThreads = 256;
 constexpr int kDeltaSamples = 4096;
+constexpr int kSlice = 128;  // edges of a work-item slice: four per lane of one warp
+static_assert(kSlice == 4 * 32, "a slice is one relax4 step of a warp");
 
 struct SsspArgs {
   const int* __restrict__ nindex;
@@ -57,16 +65,26 @@ struct SsspArgs {
   long long delta;       // > 0: fixed bucket width
   int delta_scale;
   int heavy_split;       // 1: light/heavy edge split (heavy edges relaxed once per bucket)
+  int window_scale;      // window constant C = mean weight * window_scale (0: no window)
+  int window_degree;     // vertices of at most this degree are never deferred
 };
 
 // ctl->i32[k % 3]  size of the near queue processed by near iteration k
 // ctl->i32[3 + s]  hub count of near iteration with s = k % 3
 // ctl->i32[6 + f]  far-pile size of epoch with slot f = epoch % 3
 // ctl->i32[12 + s] frontier chunks taken beyond the first one per warp, s = k % 3
-// ctl->i32[15 + s] medium-list size of near iteration k; ctl->i32[18 + s] its entries taken
+// ctl->i32[15 + s] work-item count of near iteration k; ctl->u64[7 + s] its slices taken
+// ctl->i32[21 + s] smallest distance queued for near iteration k
 // ctl->u64[4 + f]  minimum pending distance of that epoch's pile
 // ctl->u64[0..1]   weight-sample sum / count, ctl->u64[2] bucket width
 // ctl->work        relaxations that improved a distance
+
+// Lowers *slot to the warp's smallest `v` (one atomic per warp) and resets v.
+__device__ __forceinline__ void publish_min(int& v, int* slot) {
+  const int m = __reduce_min_sync(IG_FULL, v);
+  if (ig::lane_id() == 0 && m != ig::kInf) atomicMin(slot, m);
+  v = ig::kInf;
+}
 
 __global__ void __launch_bounds__(kThreads, 4) sssp_persistent(SsspArgs a) {
   using namespace ig;
@@ -96,13 +114,16 @@ __global__ void __launch_bounds__(kThreads, 4) sssp_persistent(SsspArgs a) {
   if (gtid == 0) {
     a.qa[0] = a.src;
     ctl->u64[4] = ctl->u64[5] = ctl->u64[6] = ~0ull;
+    ctl->i32[21] = ctl->i32[22] = ctl->i32[23] = kInf;
   }
   if (!grid_sync(ctl, a.timeout_ns)) return;
 
+  const unsigned long long wcnt = ld_relaxed(&ctl->u64[1]);
+  const double mean_w = wcnt ? (double)ld_relaxed(&ctl->u64[0]) / (double)wcnt : 1.0;
+  // window constant: 0 disables the deferral
+  const long long wc = a.window_scale > 0 ? max(1LL, (long long)(mean_w * a.window_scale)) : 0;
   long long delta = a.delta;
   if (delta <= 0) {
-    const unsigned long long cnt = ld_relaxed(&ctl->u64[1]);
-    const double mean_w = cnt ? (double)ld_relaxed(&ctl->u64[0]) / (double)cnt : 1.0;
     const double mean_deg = a.nodes ? (double)a.edges / (double)a.nodes : 1.0;
     delta = (long long)(mean_w * a.delta_scale / (mean_deg > 1.0 ? mean_deg : 1.0));
     if (delta < 1) delta = 1;
@@ -114,6 +135,10 @@ __global__ void __launch_bounds__(kThreads, 4) sssp_persistent(SsspArgs a) {
   int cur_size = 1;
   long long T = delta;  // distances < T are near
   int it = 0;           // near iteration index (stamp it+1 marks the next queue)
+  int mq = 0;           // smallest distance queued for iteration it (exact or below the true one)
+  int slog = 0;         // log2 of the slices per work item
+  while ((kSlice << slog) < a.item_edges) slog++;
+  int nmin = kInf;      // this thread's smallest distance queued for the next iteration
   int epoch = 0;
   int mpass = 0;        // heavy passes done
   long long improved = 0, frontier_v = 0, frontier_e = 0;
@@ -134,7 +159,8 @@ __global__ void __launch_bounds__(kThreads, 4) sssp_persistent(SsspArgs a) {
         ctl->i32[3 + (it + 1) % 3] = 0;
         ctl->i32[12 + (it + 1) % 3] = 0;
         ctl->i32[15 + (it + 1) % 3] = 0;
-        ctl->i32[18 + (it + 1) % 3] = 0;
+        ctl->u64[7 + (it + 1) % 3] = 0;
+        ctl->i32[21 + (it + 2) % 3] = kInf;
         if (heavy) ctl->i32[9 + (mpass + 1) % 2] = 0;
       }
       int* qsize = &ctl->i32[(it + 1) % 3];
@@ -167,32 +193,35 @@ __global__ void __launch_bounds__(kThreads, 4) sssp_persistent(SsspArgs a) {
           cand[k] = act[k] && du[k] != kInf && light != heavy && (long long)du[k] + w[k] < (long long)dv[k];
           old[k] = cand[k] ? atomicMin(&a.dist[v[k]], du[k] + w[k]) : 0;
         }
-        int nq[4], fq[4];
-        int nn = 0, nf = 0;
+        bool tn[4], tf[4];
 #pragma unroll
         for (int k = 0; k < 4; k++) {
+          tn[k] = tf[k] = false;
           if (cand[k] && du[k] + w[k] < old[k]) {
             improved++;
             const long long nd = (long long)du[k] + w[k];
             if (nd < T) {
-              if (a.stamp[v[k]] != next_stamp && atomicExch(&a.stamp[v[k]], next_stamp) != next_stamp)
-                nq[nn++] = v[k];
-            } else if (a.farflag[v[k]] != far_mark && atomicExch(&a.farflag[v[k]], far_mark) != far_mark) {
-              fq[nf++] = v[k];
+              nmin = min(nmin, (int)nd);
+              tn[k] = a.stamp[v[k]] != next_stamp && atomicExch(&a.stamp[v[k]], next_stamp) != next_stamp;
+            } else {
+              tf[k] = a.farflag[v[k]] != far_mark && atomicExch(&a.farflag[v[k]], far_mark) != far_mark;
             }
           }
         }
-        warp_buf_append2<4>(nn, nq, nbuf, nbuf_n, nxt, qsize, nf, fq, fbuf, fbuf_n, far, fsize, a.nodes, ctl);
+        warp_buf_append2_flags<4>(v, tn, nbuf, nbuf_n, nxt, qsize, tf, fbuf, fbuf_n, far, fsize, a.nodes, ctl);
       };
       // first chunk by warp index, the rest taken from a per-round counter so
       // that warps that drew light chunks take more (the round ends at the
-      // grid barrier, so the slowest warp sets its length)
+      // grid barrier, so the slowest warp sets its length).  A chunk is 32
+      // queue entries, fewer when the queue has less than 32 per warp, so a
+      // small round's lists are spread over the whole grid.
       int* grab = &ctl->i32[12 + it % 3];
-      for (int base = warp_g * 32; base < fcount;) {
+      const int cs = fcount >= nwarps * 32 ? 32 : max(1, (fcount + nwarps - 1) / nwarps);
+      for (int base = warp_g * cs; base < fcount;) {
         const int i = base + lane;
         int u = 0, beg = 0, deg = 0, du = kInf;
-        bool expand = false;
-        if (i < fcount) {
+        bool expand = false, defer = false;
+        if (lane < cs && i < fcount) {
           u = frontier[i];
           du = a.dist[u];
           if (heavy) {
@@ -201,14 +230,25 @@ __global__ void __launch_bounds__(kThreads, 4) sssp_persistent(SsspArgs a) {
           } else if (du < a.expanded[u]) {
             // a vertex improved while already queued is queued again; expand
             // it only if its distance dropped since its last expansion
-            a.expanded[u] = du;
             expand = true;
           }
           if (expand) {
             beg = __ldg(&a.nindex[u]);
             deg = __ldg(&a.nindex[u + 1]) - beg;
+            if (!heavy) {
+              // (du - mq) * deg >= C: outside the window, queued again
+              if (wc > 0 && deg > a.window_degree && (long long)(du - mq) * deg >= wc) {
+                expand = false;
+                deg = 0;
+                nmin = min(nmin, du);
+                defer = a.stamp[u] != next_stamp && atomicExch(&a.stamp[u], next_stamp) != next_stamp;
+              } else {
+                a.expanded[u] = du;
+              }
+            }
           }
         }
+        warp_append(defer, u, nxt, qsize, a.nodes, ctl);
         if (a.heavy_split && !heavy)
           warp_append(expand && atomicExch(&a.inmember[u], 1) == 0, u, a.members, nmembers, a.nodes, ctl);
         // a list longer than warp_degree becomes work items of item_edges
@@ -249,49 +289,63 @@ __global__ void __launch_bounds__(kThreads, 4) sssp_persistent(SsspArgs a) {
           relax4(act, e, duj);
         });
         int nb = 0;
-        if (lane == 0) nb = nwarps * 32 + atomicAdd(grab, 32);
+        if (lane == 0) nb = nwarps * cs + atomicAdd(grab, cs);
         base = __shfl_sync(IG_FULL, nb, 0);
       }
       warp_buf_flush(nbuf, nbuf_n, nxt, qsize, a.nodes, ctl);
       warp_buf_flush(fbuf, fbuf_n, far, fsize, a.nodes, ctl);
+      publish_min(nmin, &ctl->i32[21 + (it + 1) % 3]);
       if (!grid_sync(ctl, a.timeout_ns)) return;
       const int nm = ld_relaxed(&ctl->i32[15 + it % 3]);
       if (nm > 0) {
-        // work items (vertex, chunk of item_edges edges), one whole warp each
-        // over a contiguous range (no owner search), four at a time taken
-        // from a counter after the first four by warp index; the vertex's
-        // distance is read when its item starts
-        int* mgrab = &ctl->i32[18 + it % 3];
-        for (int m0 = warp_g * 4; m0 < nm;) {
-          for (int mi = m0; mi < min(m0 + 4, nm); mi++) {
-            const int u = a.mlist[mi];
-            const int du = a.dist[u];
-            const int b0 = __ldg(&a.nindex[u]), d0 = __ldg(&a.nindex[u + 1]) - b0;
-            const int off0 = a.mchunk[mi] * a.item_edges;
-            const int b = b0 + off0, d = min(a.item_edges, d0 - off0);
-            for (int base = 0; base < d; base += 128) {
-              bool act[4];
-              int e[4], duk[4];
-#pragma unroll
-              for (int k = 0; k < 4; k++) {
-                const int off = base + k * 32 + lane;
-                act[k] = off < d;
-                e[k] = b + (act[k] ? off : 0);
-                duk[k] = du;
-              }
-              relax4(act, e, duk);
+        // work items (vertex, chunk of item_edges edges) cut in slices of
+        // kSlice edges, 2^slog slices per item (the last ones of a short
+        // chunk are empty); one whole warp per slice over a contiguous range
+        // (no owner search).  Slices are taken g at a time from a counter
+        // after the first g by warp index, g sized so that every warp takes
+        // several (balance) while a large round needs few atomics; the
+        // vertex's distance is read when its item starts.
+        unsigned long long* mgrab = &ctl->u64[7 + it % 3];
+        const long long units = (long long)nm << slog;
+        const int g = (int)min(8LL, max(1LL, units / (4LL * nwarps)));
+        int cached = -1, du = kInf, b = 0, d = 0;
+        for (long long j0 = (long long)warp_g * g; j0 < units;) {
+          const long long j1 = min(j0 + g, units);
+          for (long long j = j0; j < j1; j++) {
+            const int mi = (int)(j >> slog);
+            if (mi != cached) {
+              const int u = a.mlist[mi];
+              du = a.dist[u];
+              const int b0 = __ldg(&a.nindex[u]), d0 = __ldg(&a.nindex[u + 1]) - b0;
+              const int off0 = a.mchunk[mi] * a.item_edges;
+              b = b0 + off0;
+              d = min(a.item_edges, d0 - off0);
+              cached = mi;
             }
+            const int s0 = (int)(j & ((1LL << slog) - 1)) * kSlice;
+            bool act[4];
+            int e[4], duk[4];
+#pragma unroll
+            for (int k = 0; k < 4; k++) {
+              const int off = s0 + k * 32 + lane;
+              act[k] = off < d;
+              e[k] = b + (act[k] ? off : 0);
+              duk[k] = du;
+            }
+            relax4(act, e, duk);
           }
-          int nb = 0;
-          if (lane == 0) nb = nwarps * 4 + atomicAdd(mgrab, 4);
-          m0 = __shfl_sync(IG_FULL, nb, 0);
+          unsigned long long nb = 0;
+          if (lane == 0) nb = (unsigned long long)nwarps * g + atomicAdd(mgrab, (unsigned long long)g);
+          j0 = (long long)__shfl_sync(IG_FULL, nb, 0);
         }
         warp_buf_flush(nbuf, nbuf_n, nxt, qsize, a.nodes, ctl);
         warp_buf_flush(fbuf, fbuf_n, far, fsize, a.nodes, ctl);
+        publish_min(nmin, &ctl->i32[21 + (it + 1) % 3]);
         if (!grid_sync(ctl, a.timeout_ns)) return;
       }
       if (heavy) mpass++;
       cur_size = ld_relaxed(qsize);
+      mq = ld_relaxed(&ctl->i32[21 + (it + 1) % 3]);
       nmem = a.heavy_split ? ld_relaxed(&ctl->i32[9 + mpass % 2]) : 0;
       it++;
       int* t = cur;
@@ -324,6 +378,8 @@ __global__ void __launch_bounds__(kThreads, 4) sssp_persistent(SsspArgs a) {
       const long long T_old = T;
       if (mfar != ~0ull) T = ((long long)mfar > T ? (long long)mfar : T) + delta;
       else T = T + delta;
+      // the next near queue holds distances in [T_old, T): its minimum is mfar
+      mq = mfar != ~0ull ? (int)mfar : kInf;
       int* qsize = &ctl->i32[it % 3];
       int* fsize_next = &ctl->i32[6 + (epoch + 1) % 3];
       for (long long base = gtid & ~31LL; base < fsz; base += gthreads) {
@@ -388,7 +444,8 @@ int igk_sssp(IgExec* ex, const ig_csr* dg, int src, int* d_dist) {
              (int*)mchunk, mcap,
              (int*)expanded, (int*)members, (int*)inmember, ex->d_ctl, ex->timeout_ns, o.sssp_item_edges,
              o.sssp_warp_degree,
-             o.sssp_delta, o.sssp_delta_scale, o.sssp_heavy_split};
+             o.sssp_delta, o.sssp_delta_scale, o.sssp_heavy_split, o.sssp_window_scale,
+             o.sssp_window_degree};
   void* args[] = {&a};
   return ig_launch_coop(ex, (const void*)sssp_persistent, kThreads, 0, o.blocks_per_sm, args, nullptr);
 }

@@ -32,8 +32,8 @@ import indigo_gb300 as ig  # noqa: E402
 # default, so the first variant is the default configuration.
 AXES = {
     "bfs": {"blocks_per_sm": [4, 2, 8], "hub_degree": [256, 64, 1024], "bfs_alpha": [14, 1000000]},
-    "sssp": {"blocks_per_sm": [4, 3], "sssp_item_edges": [256, 512], "sssp_warp_degree": [64, 128],
-             "sssp_delta_scale": [128, 32], "sssp_heavy_split": [0, 1]},
+    "sssp": {"blocks_per_sm": [4, 3], "sssp_item_edges": [256, 512], "sssp_window_scale": [8, 4, 0],
+             "sssp_window_degree": [16, 64], "sssp_delta_scale": [128, 32], "sssp_heavy_split": [0, 1]},
     "cc": {"blocks_per_sm": [4, 8], "hub_degree": [256, 64, 4096]},
     "mis": {"blocks_per_sm": [4, 2, 8]},
     "pr": {"pr_blocks_per_sm": [3, 2, 4], "pr_hub_degree": [1024, 256, 4096], "pr_chunk": [4096, 512]},
@@ -41,7 +41,8 @@ AXES = {
 }
 # short labels for the variant names (like the suite's style words)
 LABEL = {"blocks_per_sm": "B", "hub_degree": "Hub", "bfs_alpha": "Alpha", "sssp_item_edges": "Item",
-         "sssp_warp_degree": "Warp", "sssp_delta_scale": "Delta", "sssp_heavy_split": "Split", "pr_blocks_per_sm": "B",
+         "sssp_warp_degree": "Warp", "sssp_window_scale": "Win", "sssp_window_degree": "WinDeg",
+         "sssp_delta_scale": "Delta", "sssp_heavy_split": "Split", "pr_blocks_per_sm": "B",
          "pr_hub_degree": "Hub", "pr_chunk": "Chunk", "tc_block_chunk": "Item"}
 
 
@@ -126,8 +127,9 @@ def result(algo, g, out, scores, cnt):
 def sweep(g, algos, repeat: int, graph_name: str, log=print) -> dict:
     gd = g.degree_ordered() if "tc" in algos else None
     src = int(g.pick_sources(1, seed=7)[0])
-    names = ("blocks_per_sm", "hub_degree", "bfs_alpha", "sssp_item_edges", "sssp_warp_degree", "sssp_delta_scale",
-             "sssp_heavy_split", "pr_blocks_per_sm", "pr_hub_degree", "pr_chunk", "tc_block_chunk")
+    names = ("blocks_per_sm", "hub_degree", "bfs_alpha", "sssp_item_edges", "sssp_warp_degree", "sssp_window_scale",
+             "sssp_window_degree", "sssp_delta_scale", "sssp_heavy_split", "pr_blocks_per_sm", "pr_hub_degree",
+             "pr_chunk", "tc_block_chunk")
     saved = {k: ig.get_option(k) for k in names}
     rows = {}
     with ig.DeviceCSR(g) as d:
