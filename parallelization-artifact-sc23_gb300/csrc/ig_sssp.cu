@@ -172,9 +172,14 @@ __global__ void __launch_bounds__(kThreads, 4) sssp_persistent(SsspArgs a) {
       const int* frontier = heavy ? a.members : cur;
       const int fcount = heavy ? nmem : cur_size;
       // Four edges per lane at a time: their loads, atomics and stamp checks
-      // are independent, so they are issued together.
+      // are independent, so they are issued together.  The distance update is
+      // a reduction (atomicMin without a result): an edge whose candidate beats
+      // the distance it read counts as an improvement without waiting for the
+      // atomic.  Another edge may have lowered the distance further in the
+      // meantime; the vertex is then queued once more than needed (the stamp
+      // keeps it to one entry per queue, the expanded-distance check skips it).
       auto relax4 = [&](const bool (&act)[4], const int (&e)[4], const int (&du)[4]) {
-        int v[4], w[4], dv[4], old[4];
+        int v[4], w[4], dv[4], sv[4];
         bool cand[4];
 #pragma unroll
         for (int k = 0; k < 4; k++) {
@@ -191,18 +196,20 @@ __global__ void __launch_bounds__(kThreads, 4) sssp_persistent(SsspArgs a) {
         for (int k = 0; k < 4; k++) {
           const bool light = !a.heavy_split || (long long)w[k] < delta;
           cand[k] = act[k] && du[k] != kInf && light != heavy && (long long)du[k] + w[k] < (long long)dv[k];
-          old[k] = cand[k] ? atomicMin(&a.dist[v[k]], du[k] + w[k]) : 0;
+          if (cand[k]) atomicMin(&a.dist[v[k]], du[k] + w[k]);
         }
+#pragma unroll
+        for (int k = 0; k < 4; k++) sv[k] = cand[k] ? a.stamp[v[k]] : 0;
         bool tn[4], tf[4];
 #pragma unroll
         for (int k = 0; k < 4; k++) {
           tn[k] = tf[k] = false;
-          if (cand[k] && du[k] + w[k] < old[k]) {
+          if (cand[k]) {
             improved++;
             const long long nd = (long long)du[k] + w[k];
             if (nd < T) {
               nmin = min(nmin, (int)nd);
-              tn[k] = a.stamp[v[k]] != next_stamp && atomicExch(&a.stamp[v[k]], next_stamp) != next_stamp;
+              tn[k] = sv[k] != next_stamp && atomicExch(&a.stamp[v[k]], next_stamp) != next_stamp;
             } else {
               tf[k] = a.farflag[v[k]] != far_mark && atomicExch(&a.farflag[v[k]], far_mark) != far_mark;
             }
@@ -223,18 +230,21 @@ __global__ void __launch_bounds__(kThreads, 4) sssp_persistent(SsspArgs a) {
         bool expand = false, defer = false;
         if (lane < cs && i < fcount) {
           u = frontier[i];
+          // every per-vertex read depends only on u, so they are issued together
           du = a.dist[u];
+          const int ex = heavy ? kInf : a.expanded[u];
+          beg = __ldg(&a.nindex[u]);
+          const int end = __ldg(&a.nindex[u + 1]);
           if (heavy) {
             a.inmember[u] = 0;
             expand = true;
-          } else if (du < a.expanded[u]) {
+          } else {
             // a vertex improved while already queued is queued again; expand
             // it only if its distance dropped since its last expansion
-            expand = true;
+            expand = du < ex;
           }
           if (expand) {
-            beg = __ldg(&a.nindex[u]);
-            deg = __ldg(&a.nindex[u + 1]) - beg;
+            deg = end - beg;
             if (!heavy) {
               // (du - mq) * deg >= C: outside the window, queued again
               if (wc > 0 && deg > a.window_degree && (long long)(du - mq) * deg >= wc) {
@@ -246,37 +256,30 @@ __global__ void __launch_bounds__(kThreads, 4) sssp_persistent(SsspArgs a) {
                 a.expanded[u] = du;
               }
             }
+
           }
         }
-        warp_append(defer, u, nxt, qsize, a.nodes, ctl);
+        {
+          const int dq[1] = {u};
+          warp_buf_append<1>(defer ? 1 : 0, dq, nbuf, nbuf_n, nxt, qsize, a.nodes, ctl);
+        }
         if (a.heavy_split && !heavy)
           warp_append(expand && atomicExch(&a.inmember[u], 1) == 0, u, a.members, nmembers, a.nodes, ctl);
         // a list longer than warp_degree becomes work items of item_edges
-        // edges each, expanded after the barrier one warp per item
+        // edges each, expanded after the barrier; the slots are reserved here
+        // and written after the chunk's short lists, so the reservation's
+        // round trip overlaps them
         const bool listed = deg > a.warp_degree;
-        {
-          const int cnt = listed ? (deg + a.item_edges - 1) / a.item_edges : 0;
-          int incl = cnt;
+        const int cnt = listed ? (deg + a.item_edges - 1) / a.item_edges : 0;
+        int incl = cnt;
 #pragma unroll
-          for (int o = 1; o < 32; o <<= 1) {
-            const int t = __shfl_up_sync(IG_FULL, incl, o);
-            if (lane >= o) incl += t;
-          }
-          const int total = __shfl_sync(IG_FULL, incl, 31);
-          if (total > 0) {
-            int ibase = 0;
-            if (lane == 31) ibase = atomicAdd(&ctl->i32[15 + it % 3], total);
-            ibase = __shfl_sync(IG_FULL, ibase, 31) + incl - cnt;
-            for (int c = 0; c < cnt; c++) {
-              if (ibase + c < a.mcap) {
-                a.mlist[ibase + c] = u;
-                a.mchunk[ibase + c] = c;
-              } else {
-                raise(ctl, IG_ERR_OVERFLOW);
-              }
-            }
-          }
+        for (int o = 1; o < 32; o <<= 1) {
+          const int t = __shfl_up_sync(IG_FULL, incl, o);
+          if (lane >= o) incl += t;
         }
+        const int itotal = __shfl_sync(IG_FULL, incl, 31);
+        int ibase = 0;
+        if (itotal > 0 && lane == 31) ibase = atomicAdd(&ctl->i32[15 + it % 3], itotal);
         if (expand) {
           frontier_v++;
           frontier_e += deg;
@@ -288,6 +291,31 @@ __global__ void __launch_bounds__(kThreads, 4) sssp_persistent(SsspArgs a) {
           for (int k = 0; k < 4; k++) duj[k] = __shfl_sync(IG_FULL, du, j[k]);
           relax4(act, e, duj);
         });
+        if (itotal > 0) {
+          // the warp writes the chunk's items together: slot idx belongs to
+          // the last lane whose exclusive count is <= idx
+          ibase = __shfl_sync(IG_FULL, ibase, 31);
+          const int excl = incl - cnt;
+          for (int i0 = 0; i0 < itotal; i0 += 32) {
+            const int idx = i0 + lane;
+            int j = 0;
+#pragma unroll
+            for (int step = 16; step >= 1; step >>= 1) {
+              const int ej = __shfl_sync(IG_FULL, excl, j + step);
+              if (ej <= idx) j += step;
+            }
+            const int uj = __shfl_sync(IG_FULL, u, j);
+            const int c = idx - __shfl_sync(IG_FULL, excl, j);
+            if (idx < itotal) {
+              if (ibase + idx < a.mcap) {
+                a.mlist[ibase + idx] = uj;
+                a.mchunk[ibase + idx] = c;
+              } else {
+                raise(ctl, IG_ERR_OVERFLOW);
+              }
+            }
+          }
+        }
         int nb = 0;
         if (lane == 0) nb = nwarps * cs + atomicAdd(grab, cs);
         base = __shfl_sync(IG_FULL, nb, 0);
@@ -304,24 +332,31 @@ __global__ void __launch_bounds__(kThreads, 4) sssp_persistent(SsspArgs a) {
         // (no owner search).  Slices are taken g at a time from a counter
         // after the first g by warp index, g sized so that every warp takes
         // several (balance) while a large round needs few atomics; the
-        // vertex's distance is read when its item starts.
+        // vertex's distance is read when its group starts.
         unsigned long long* mgrab = &ctl->u64[7 + it % 3];
         const long long units = (long long)nm << slog;
         const int g = (int)min(8LL, max(1LL, units / (4LL * nwarps)));
-        int cached = -1, du = kInf, b = 0, d = 0;
         for (long long j0 = (long long)warp_g * g; j0 < units;) {
           const long long j1 = min(j0 + g, units);
+          // the group's items (at most g): lane t reads item mfirst + t, so
+          // the headers of the group load together
+          const int mfirst = (int)(j0 >> slog);
+          const int ni = (int)((j1 - 1) >> slog) - mfirst + 1;
+          int hdu = kInf, hb = 0, hd = 0;
+          if (lane < ni) {
+            const int mi = mfirst + lane;
+            const int u = a.mlist[mi];
+            hdu = a.dist[u];
+            const int b0 = __ldg(&a.nindex[u]), d0 = __ldg(&a.nindex[u + 1]) - b0;
+            const int off0 = a.mchunk[mi] * a.item_edges;
+            hb = b0 + off0;
+            hd = min(a.item_edges, d0 - off0);
+          }
           for (long long j = j0; j < j1; j++) {
-            const int mi = (int)(j >> slog);
-            if (mi != cached) {
-              const int u = a.mlist[mi];
-              du = a.dist[u];
-              const int b0 = __ldg(&a.nindex[u]), d0 = __ldg(&a.nindex[u + 1]) - b0;
-              const int off0 = a.mchunk[mi] * a.item_edges;
-              b = b0 + off0;
-              d = min(a.item_edges, d0 - off0);
-              cached = mi;
-            }
+            const int t = (int)(j >> slog) - mfirst;
+            const int du = __shfl_sync(IG_FULL, hdu, t);
+            const int b = __shfl_sync(IG_FULL, hb, t);
+            const int d = __shfl_sync(IG_FULL, hd, t);
             const int s0 = (int)(j & ((1LL << slog) - 1)) * kSlice;
             bool act[4];
             int e[4], duk[4];
