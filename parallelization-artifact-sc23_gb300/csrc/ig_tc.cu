@@ -19,7 +19,12 @@
 //               otherwise) and every w of the out-lists N+(u) is probed
 //               (load-balanced warp expansion, four probes per lane in
 //               flight); a hit is the triangle u -> v -> w, counted once (at
-//               its middle vertex).  Work: sum over u of |N+(u)|^2 probes,
+//               its middle vertex).  When the ids are in (degree, id) order
+//               every w of N+(v) is above v, and a middle vertex with a long
+//               N+(v) sits near the top of the id range: if fewer than 2^17
+//               ids lie above v, N+(v) is an exact bitmap over (v, V) in the
+//               block's shared memory instead (one bit test per probe, no
+//               filter and no hash walk).  Work: sum over u of |N+(u)|^2 probes,
 //               halved when the ids are already in (degree, id) order (the
 //               degree-ordered input of the benchmark): then only the part
 //               of N+(u) after v is scanned.  The filter rejects most misses
@@ -39,6 +44,8 @@ constexpr int kBitWords = 256;    // block filter: 8192 bits, bit (w mod 8192) s
 constexpr int kWarpCap = 128;     // warp table slots (out-degree <= kBlockOut)
 constexpr int kWarpBitWords = 64; // warp filter: 2048 bits
 constexpr int kWarpList = 96;     // in-neighbour lists this long are walked by the whole warp
+constexpr int kSpanWords = 4096;  // block bitmap: 131072 bits, bit (w - v - 1) set for w in N+(v)
+static_assert(kSpanWords >= kHashCap + kBitWords, "the bitmap shares its memory with the table and filter");
 
 // Work items of middle vertex v with `out` out-neighbours and `in`
 // in-neighbours: warp items of kChunk in-neighbours for a short N+(v), block
@@ -237,11 +244,12 @@ __global__ void __launch_bounds__(kThreads) tc_item_owner(const int* __restrict_
 
 // Probes of one group of <= 32 in-neighbours u of middle vertex v, one per
 // lane (in_list[g .. gend)): every w of N+(u) (only the part after v when ids
-// are in (degree, id) order) is looked up in N+(v): filter bit first, then the
-// hash table (or a binary search of N+(v) when it was too long to hash).  A
-// hit closes the triangle u -> v -> w, counted once at v.  Returns this lane's
-// hits.  All lanes of the warp call it.
-template <int kBits>
+// are in (degree, id) order) is looked up in N+(v): with kExact in the bitmap
+// `bits` over ids v+1 ..; otherwise filter bit first, then the hash table (or
+// a binary search of N+(v) when it was too long to hash).  A hit closes the
+// triangle u -> v -> w, counted once at v.  Returns this lane's hits.  All
+// lanes of the warp call it.
+template <int kBits, bool kExact = false>
 __device__ __forceinline__ unsigned long long probe_group(const int* __restrict__ out_off,
                                                           const int* __restrict__ out_list,
                                                           const int* __restrict__ in_list, int g, int gend, int v,
@@ -270,6 +278,10 @@ __device__ __forceinline__ unsigned long long probe_group(const int* __restrict_
   // membership of w in N+(v): filter bit first (rejects most misses with one
   // shared load), then the hash table or a binary search of N+(v)
   auto probe = [&](int w) -> int {
+    if (kExact) {
+      const unsigned x = (unsigned)(w - v - 1);  // w > v: only the part of N+(u) after v is scanned
+      return (bits[x >> 5] >> (x & 31)) & 1u;
+    }
     if (hashed) {
       if (((bits[(w >> 5) & (kBits - 1)] >> (w & 31)) & 1u) == 0) return 0;
       unsigned h = hash_slot(w, mask);
@@ -404,8 +416,11 @@ __global__ void __launch_bounds__(kThreads) tc_count_warp(const int* __restrict_
 // block_chunk of its in-neighbours).  The block hashes N+(v) once into one
 // shared table (9 KB instead of a 9 KB table per warp, so eight blocks fit
 // on an SM) and its warps take groups of 32 in-neighbours from a shared
-// counter until the item is done.
-template <bool kBatched>
+// counter until the item is done.  kExact: this launch takes the items whose
+// N+(v) fits the exact bitmap (ids in (degree, id) order and fewer than 2^17
+// ids above v) and the other launch the rest, so each path gets its own
+// register allocation.
+template <bool kBatched, bool kExact>
 __global__ void __launch_bounds__(kThreads, 8) tc_count_block(const int* __restrict__ out_off,
                                                               const int* __restrict__ out_list,
                                                               const int* __restrict__ nindex,
@@ -416,9 +431,11 @@ __global__ void __launch_bounds__(kThreads, 8) tc_count_block(const int* __restr
                                                               const int* __restrict__ graph_vptr, int graphs,
                                                               int block_chunk) {
   using namespace ig;
-  __shared__ int tab[kHashCap];
-  __shared__ unsigned bits[kBitWords];
+  // the exact bitmap, or the hash table followed by the filter
+  __shared__ unsigned s_mem[kExact ? kSpanWords : kHashCap + kBitWords];
   __shared__ int s_next;
+  int* tab = (int*)s_mem;
+  unsigned* bits = s_mem + kHashCap;
   if (ctl->err) return;
   const int lane = lane_id();
   const int items = __ldg(&item_off[n]);
@@ -429,13 +446,23 @@ __global__ void __launch_bounds__(kThreads, 8) tc_count_block(const int* __restr
   bool hashed = false;
   for (int it = blockIdx.x; it < items; it += gridDim.x) {
     const int v = __ldg(&item_v[it]);  // middle vertex (block-uniform)
+    const int span = n - 1 - v;        // ids above v
+    if ((ranked && span <= kSpanWords * 32) != kExact) continue;  // the other launch's item
     const int vb = __ldg(&out_off[v]);
     const int vd = __ldg(&out_off[v + 1]) - vb;
     __syncthreads();  // the previous item's probes are done with the table and the counter
     if (v != cur_v) {
       cur_v = v;
-      hashed = 2 * vd <= kHashCap;
-      if (hashed) {
+      hashed = !kExact && 2 * vd <= kHashCap;
+      if (kExact) {
+        const int words = (span + 31) >> 5;
+        for (int k = threadIdx.x; k < words; k += blockDim.x) s_mem[k] = 0u;
+        __syncthreads();
+        for (int k = threadIdx.x; k < vd; k += blockDim.x) {
+          const unsigned x = (unsigned)(__ldg(&out_list[vb + k]) - v - 1);
+          atomicOr(&s_mem[x >> 5], 1u << (x & 31));
+        }
+      } else if (hashed) {
         int cap = 32;
         while (cap < 2 * vd) cap <<= 1;
         mask = (unsigned)cap - 1;
@@ -462,8 +489,12 @@ __global__ void __launch_bounds__(kThreads, 8) tc_count_block(const int* __restr
       if (lane == 0) g = atomicAdd(&s_next, 32);
       g = c0 + __shfl_sync(IG_FULL, g, 0);
       if (g >= c1) break;
-      local += probe_group<kBitWords>(out_off, out_list, in_list, g, c1, v, vb, vd, ranked, tab, bits, mask,
-                                      hashed);
+      if constexpr (kExact)
+        local += probe_group<kBitWords, true>(out_off, out_list, in_list, g, c1, v, vb, vd, true, tab, s_mem, mask,
+                                              false);
+      else
+        local += probe_group<kBitWords>(out_off, out_list, in_list, g, c1, v, vb, vd, ranked, tab, bits, mask,
+                                        hashed);
     }
     if (kBatched) tc_add_graph(local - before_item, count, graph_vptr, graphs, v);
   }
@@ -534,22 +565,26 @@ static int tc_run(IgExec* ex, int nodes, int edges, const int* d_nindex, const i
   tc_item_owner<<<grid, kThreads, 0, ex->stream>>>((const int*)ioff_b, nodes, (int*)itemv_b);
   const int cgrid = ex->sms * 8;
   if (d_graph_vptr) {
-    tc_count_block<true><<<cgrid, kThreads, 0, ex->stream>>>((const int*)off, (const int*)list, d_nindex,
-                                                             (const int*)inl, (const int*)ioff_b,
-                                                             (const int*)itemv_b, nodes, d_count, ex->d_ctl,
-                                                             d_graph_vptr, graphs, block_chunk);
+    tc_count_block<true, true><<<cgrid, kThreads, 0, ex->stream>>>(
+        (const int*)off, (const int*)list, d_nindex, (const int*)inl, (const int*)ioff_b, (const int*)itemv_b, nodes,
+        d_count, ex->d_ctl, d_graph_vptr, graphs, block_chunk);
+    tc_count_block<true, false><<<cgrid, kThreads, 0, ex->stream>>>(
+        (const int*)off, (const int*)list, d_nindex, (const int*)inl, (const int*)ioff_b, (const int*)itemv_b, nodes,
+        d_count, ex->d_ctl, d_graph_vptr, graphs, block_chunk);
     tc_count_warp<true><<<cgrid, kThreads, 0, ex->stream>>>((const int*)off, (const int*)list, d_nindex,
                                                             (const int*)inl, (const int*)ioff, (const int*)itemv,
                                                             nodes, d_count, ex->d_ctl, d_graph_vptr, graphs);
   } else {
-    tc_count_block<false><<<cgrid, kThreads, 0, ex->stream>>>((const int*)off, (const int*)list, d_nindex,
-                                                              (const int*)inl, (const int*)ioff_b,
-                                                              (const int*)itemv_b, nodes, d_count, ex->d_ctl,
-                                                              nullptr, 0, block_chunk);
+    tc_count_block<false, true><<<cgrid, kThreads, 0, ex->stream>>>(
+        (const int*)off, (const int*)list, d_nindex, (const int*)inl, (const int*)ioff_b, (const int*)itemv_b, nodes,
+        d_count, ex->d_ctl, nullptr, 0, block_chunk);
+    tc_count_block<false, false><<<cgrid, kThreads, 0, ex->stream>>>(
+        (const int*)off, (const int*)list, d_nindex, (const int*)inl, (const int*)ioff_b, (const int*)itemv_b, nodes,
+        d_count, ex->d_ctl, nullptr, 0, block_chunk);
     tc_count_warp<false><<<cgrid, kThreads, 0, ex->stream>>>((const int*)off, (const int*)list, d_nindex,
                                                              (const int*)inl, (const int*)ioff, (const int*)itemv,
                                                              nodes, d_count, ex->d_ctl, nullptr, 0);
   }
-  ig_count_launches(8);
+  ig_count_launches(9);
   return ig_cuda_check((int)cudaGetLastError(), "tc launch");
 }
