@@ -45,8 +45,9 @@ struct BfsArgs {
   int nsources;
 };
 
-// ctl->i32[s] : size of the queue built during a level with slot s (= level % 3)
-// ctl->i32[3 + s]: hub count, ctl->u64[s]: sum of degrees of the queued vertices
+// Hot counters of the control block, slot s = level % 3: hot32(s) size of the
+// queue built during the level, hot32(3 + s) its hub count, hot64(6 + s) the
+// sum of degrees of the queued vertices.
 
 __global__ void __launch_bounds__(kThreads) bfs_persistent(BfsArgs a) {
   using namespace ig;
@@ -86,13 +87,13 @@ __global__ void __launch_bounds__(kThreads) bfs_persistent(BfsArgs a) {
     const int slot = level % 3;
     if (gtid == 0) {
       const int ns = (level + 1) % 3;
-      ctl->i32[ns] = 0;
-      ctl->i32[3 + ns] = 0;
-      ctl->u64[ns] = 0;
+      *hot32(ctl, ns) = 0;
+      *hot32(ctl, 3 + ns) = 0;
+      *hot64(ctl, 6 + ns) = 0;
     }
-    int* qsize = &ctl->i32[slot];
-    int* nhub = &ctl->i32[3 + slot];
-    unsigned long long* fedges = &ctl->u64[slot];
+    int* qsize = hot32(ctl, slot);
+    int* nhub = hot32(ctl, 3 + slot);
+    unsigned long long* fedges = hot64(ctl, 6 + slot);
     const int next_level = level + 1;
 
     if (!bottom_up) {

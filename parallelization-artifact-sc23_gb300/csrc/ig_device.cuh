@@ -69,6 +69,12 @@ __device__ __forceinline__ double ld_relaxed(const double* p) {
   return v;
 }
 
+// Hot counter k of the control block (see IgCtl::hot), as int or 64-bit.
+__device__ __forceinline__ int* hot32(IgCtl* ctl, int k) { return &ctl->hot[k * kCtlSpread]; }
+__device__ __forceinline__ unsigned long long* hot64(IgCtl* ctl, int k) {
+  return (unsigned long long*)&ctl->hot[k * kCtlSpread];
+}
+
 // Records the first device-side error.
 __device__ __forceinline__ void raise(IgCtl* ctl, int code) { atomicCAS(&ctl->err, 0, code); }
 

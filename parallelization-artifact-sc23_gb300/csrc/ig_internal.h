@@ -30,18 +30,28 @@ struct IgSync {
   unsigned int gen;
 };
 
+// Counters that every warp of a persistent kernel updates with atomics
+// (queue sizes, work grabs, round minima) sit 256 bytes apart: packed into one
+// line they all queue in one L2 slice, together with the grid barrier's flag
+// that every block polls.
+constexpr int kCtlHot = 24;     // hot counters
+constexpr int kCtlSpread = 64;  // ints from one hot counter to the next
+
 struct IgCtl {
   int sticky_err;              // first error of any run since last reported (not reset per run)
   int pad_;
-  IgSync sync;                 // grid barrier state
   int err;                     // first ig_status raised on the device
   int iterations;              // levels / rounds / iterations executed
   long long work;              // algorithm-specific work counter
   double residual;             // PageRank residual of the last iteration
-  int i32[32];                 // per-algorithm integer counters
+  int i32[32];                 // per-algorithm integer counters (set a few times per call)
   unsigned long long u64[16];  // per-algorithm 64-bit counters
   double f64[8];
+  alignas(256) IgSync sync;    // grid barrier state, on a line of its own
+  alignas(256) int hot[kCtlHot * kCtlSpread];  // hot counter k at hot[k * kCtlSpread]
 };
+// The part of the control block the host reads back after a run.
+constexpr size_t kCtlHostBytes = offsetof(IgCtl, sync);
 
 // Scratch slots: each algorithm names the buffers it needs; the pool grows a
 // slot on demand and keeps it for later calls.

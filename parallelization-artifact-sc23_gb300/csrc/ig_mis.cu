@@ -69,8 +69,8 @@ __global__ void __launch_bounds__(kThreads) mis_persistent(MisArgs a) {
   int round = 0;
   while (cur_size > 0) {
     const int slot = round % 3;
-    if (gtid == 0) ctl->i32[(round + 1) % 3] = 0;
-    int* wsize = &ctl->i32[slot];
+    if (gtid == 0) *hot32(ctl, (round + 1) % 3) = 0;
+    int* wsize = hot32(ctl, slot);
     for (long long base = gtid & ~31LL; base < cur_size; base += gthreads) {
       const long long i = base + lane;
       int v = 0, beg = 0, end = 0;

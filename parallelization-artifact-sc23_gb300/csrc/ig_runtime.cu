@@ -139,7 +139,7 @@ int ig_exec_reset(IgExec* ex) {
 }
 
 int ig_exec_finish(IgExec* ex) {
-  IG_CU(cudaMemcpyAsync(ex->h_ctl, ex->d_ctl, sizeof(IgCtl), cudaMemcpyDeviceToHost, ex->stream));
+  IG_CU(cudaMemcpyAsync(ex->h_ctl, ex->d_ctl, kCtlHostBytes, cudaMemcpyDeviceToHost, ex->stream));
   IG_CU(cudaStreamSynchronize(ex->stream));
   const int err = ex->h_ctl->err;
   if (err == IG_ERR_TIMEOUT) return ig_fail(err, "a device-side wait exceeded %d ms", g_timeout_ms.load());

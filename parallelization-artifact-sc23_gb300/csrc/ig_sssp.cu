@@ -69,13 +69,21 @@ struct SsspArgs {
   int window_degree;     // vertices of at most this degree are never deferred
 };
 
-// ctl->i32[k % 3]  size of the near queue processed by near iteration k
-// ctl->i32[3 + s]  hub count of near iteration with s = k % 3
-// ctl->i32[6 + f]  far-pile size of epoch with slot f = epoch % 3
-// ctl->i32[12 + s] frontier chunks taken beyond the first one per warp, s = k % 3
-// ctl->i32[15 + s] work-item count of near iteration k; ctl->u64[7 + s] its slices taken
-// ctl->i32[21 + s] smallest distance queued for near iteration k
-// ctl->u64[4 + f]  minimum pending distance of that epoch's pile
+// Per-round counters: hot counters of the control block (every warp updates
+// them with atomics).  Slot s = k % 3 for near iteration k, f = epoch % 3 for
+// far epochs.
+enum SsspCounter : int {
+  kCQueue = 0,     // [3] size of the near queue processed by near iteration k
+  kCFar = 3,       // [3] far-pile size of epoch f
+  kCGrab = 6,      // [3] frontier chunks taken beyond the first one per warp
+  kCItems = 9,     // [3] work-item count of near iteration k
+  kCMin = 12,      // [3] smallest distance queued for near iteration k
+  kCMembers = 15,  // [2] member count (light/heavy split), slot mpass % 2
+  kCSlices = 17,   // [3] (64-bit) work-item slices taken
+  kCFarMin = 20,   // [3] (64-bit) minimum pending distance of epoch f's pile
+  kCCount = 23
+};
+static_assert(kCCount <= kCtlHot, "SSSP counters must fit the control block's hot counters");
 // ctl->u64[0..1]   weight-sample sum / count, ctl->u64[2] bucket width
 // ctl->work        relaxations that improved a distance
 
@@ -89,6 +97,8 @@ __device__ __forceinline__ void publish_min(int& v, int* slot) {
 __global__ void __launch_bounds__(kThreads, 4) sssp_persistent(SsspArgs a) {
   using namespace ig;
   IgCtl* ctl = a.ctl;
+  auto ci = [&](int k) { return hot32(ctl, k); };
+  auto cu = [&](int k) { return hot64(ctl, k); };
   const int lane = lane_id();
   const long long gtid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   const long long gthreads = (long long)gridDim.x * blockDim.x;
@@ -111,10 +121,10 @@ __global__ void __launch_bounds__(kThreads, 4) sssp_persistent(SsspArgs a) {
     atomicAdd(&ctl->u64[0], (unsigned long long)max(0, __ldg(&a.eweight[e])));
     atomicAdd(&ctl->u64[1], 1ull);
   }
-  if (gtid == 0) {
-    a.qa[0] = a.src;
-    ctl->u64[4] = ctl->u64[5] = ctl->u64[6] = ~0ull;
-    ctl->i32[21] = ctl->i32[22] = ctl->i32[23] = kInf;
+  if (gtid == 0) a.qa[0] = a.src;
+  if (gtid < kCCount) {
+    if (gtid >= kCSlices) *cu((int)gtid) = gtid >= kCFarMin ? ~0ull : 0ull;
+    else *ci((int)gtid) = (gtid >= kCMin && gtid < kCMin + 3) ? kInf : 0;
   }
   if (!grid_sync(ctl, a.timeout_ns)) return;
 
@@ -155,18 +165,17 @@ __global__ void __launch_bounds__(kThreads, 4) sssp_persistent(SsspArgs a) {
     while (cur_size > 0 || nmem > 0) {
       const bool heavy = cur_size == 0;
       if (gtid == 0) {
-        ctl->i32[(it + 2) % 3] = 0;
-        ctl->i32[3 + (it + 1) % 3] = 0;
-        ctl->i32[12 + (it + 1) % 3] = 0;
-        ctl->i32[15 + (it + 1) % 3] = 0;
-        ctl->u64[7 + (it + 1) % 3] = 0;
-        ctl->i32[21 + (it + 2) % 3] = kInf;
-        if (heavy) ctl->i32[9 + (mpass + 1) % 2] = 0;
+        *ci(kCQueue + (it + 2) % 3) = 0;
+        *ci(kCGrab + (it + 1) % 3) = 0;
+        *ci(kCItems + (it + 1) % 3) = 0;
+        *cu(kCSlices + (it + 1) % 3) = 0;
+        *ci(kCMin + (it + 2) % 3) = kInf;
+        if (heavy) *ci(kCMembers + (mpass + 1) % 2) = 0;
       }
-      int* qsize = &ctl->i32[(it + 1) % 3];
-      int* nmembers = &ctl->i32[9 + mpass % 2];
+      int* qsize = ci(kCQueue + (it + 1) % 3);
+      int* nmembers = ci(kCMembers + mpass % 2);
       int* far = (epoch & 1) ? a.fb : a.fa;
-      int* fsize = &ctl->i32[6 + epoch % 3];
+      int* fsize = ci(kCFar + epoch % 3);
       const int next_stamp = it + 1;
       const int far_mark = epoch + 1;
       const int* frontier = heavy ? a.members : cur;
@@ -222,7 +231,7 @@ __global__ void __launch_bounds__(kThreads, 4) sssp_persistent(SsspArgs a) {
       // grid barrier, so the slowest warp sets its length).  A chunk is 32
       // queue entries, fewer when the queue has less than 32 per warp, so a
       // small round's lists are spread over the whole grid.
-      int* grab = &ctl->i32[12 + it % 3];
+      int* grab = ci(kCGrab + it % 3);
       const int cs = fcount >= nwarps * 32 ? 32 : max(1, (fcount + nwarps - 1) / nwarps);
       for (int base = warp_g * cs; base < fcount;) {
         const int i = base + lane;
@@ -279,7 +288,7 @@ __global__ void __launch_bounds__(kThreads, 4) sssp_persistent(SsspArgs a) {
         }
         const int itotal = __shfl_sync(IG_FULL, incl, 31);
         int ibase = 0;
-        if (itotal > 0 && lane == 31) ibase = atomicAdd(&ctl->i32[15 + it % 3], itotal);
+        if (itotal > 0 && lane == 31) ibase = atomicAdd(ci(kCItems + it % 3), itotal);
         if (expand) {
           frontier_v++;
           frontier_e += deg;
@@ -322,9 +331,9 @@ __global__ void __launch_bounds__(kThreads, 4) sssp_persistent(SsspArgs a) {
       }
       warp_buf_flush(nbuf, nbuf_n, nxt, qsize, a.nodes, ctl);
       warp_buf_flush(fbuf, fbuf_n, far, fsize, a.nodes, ctl);
-      publish_min(nmin, &ctl->i32[21 + (it + 1) % 3]);
+      publish_min(nmin, ci(kCMin + (it + 1) % 3));
       if (!grid_sync(ctl, a.timeout_ns)) return;
-      const int nm = ld_relaxed(&ctl->i32[15 + it % 3]);
+      const int nm = ld_relaxed(ci(kCItems + it % 3));
       if (nm > 0) {
         // work items (vertex, chunk of item_edges edges) cut in slices of
         // kSlice edges, 2^slog slices per item (the last ones of a short
@@ -333,7 +342,7 @@ __global__ void __launch_bounds__(kThreads, 4) sssp_persistent(SsspArgs a) {
         // after the first g by warp index, g sized so that every warp takes
         // several (balance) while a large round needs few atomics; the
         // vertex's distance is read when its group starts.
-        unsigned long long* mgrab = &ctl->u64[7 + it % 3];
+        unsigned long long* mgrab = cu(kCSlices + it % 3);
         const long long units = (long long)nm << slog;
         const int g = (int)min(8LL, max(1LL, units / (4LL * nwarps)));
         for (long long j0 = (long long)warp_g * g; j0 < units;) {
@@ -375,13 +384,13 @@ __global__ void __launch_bounds__(kThreads, 4) sssp_persistent(SsspArgs a) {
         }
         warp_buf_flush(nbuf, nbuf_n, nxt, qsize, a.nodes, ctl);
         warp_buf_flush(fbuf, fbuf_n, far, fsize, a.nodes, ctl);
-        publish_min(nmin, &ctl->i32[21 + (it + 1) % 3]);
+        publish_min(nmin, ci(kCMin + (it + 1) % 3));
         if (!grid_sync(ctl, a.timeout_ns)) return;
       }
       if (heavy) mpass++;
       cur_size = ld_relaxed(qsize);
-      mq = ld_relaxed(&ctl->i32[21 + (it + 1) % 3]);
-      nmem = a.heavy_split ? ld_relaxed(&ctl->i32[9 + mpass % 2]) : 0;
+      mq = ld_relaxed(ci(kCMin + (it + 1) % 3));
+      nmem = a.heavy_split ? ld_relaxed(ci(kCMembers + mpass % 2)) : 0;
       it++;
       int* t = cur;
       cur = nxt;
@@ -393,7 +402,7 @@ __global__ void __launch_bounds__(kThreads, 4) sssp_persistent(SsspArgs a) {
     bool done = false;
     while (cur_size == 0) {
       const int f = epoch % 3;
-      const int fsz = ld_relaxed(&ctl->i32[6 + f]);
+      const int fsz = ld_relaxed(ci(kCFar + f));
       if (fsz == 0) {
         done = true;
         break;
@@ -401,22 +410,22 @@ __global__ void __launch_bounds__(kThreads, 4) sssp_persistent(SsspArgs a) {
       int* far = (epoch & 1) ? a.fb : a.fa;
       int* far_next = (epoch & 1) ? a.fa : a.fb;
       if (gtid == 0) {
-        ctl->i32[6 + (epoch + 1) % 3] = 0;
-        ctl->u64[4 + (epoch + 1) % 3] = ~0ull;
+        *ci(kCFar + (epoch + 1) % 3) = 0;
+        *cu(kCFarMin + (epoch + 1) % 3) = ~0ull;
       }
       for (long long i = gtid; i < fsz; i += gthreads) {
         const int d = a.dist[far[i]];
-        if ((long long)d >= T) atomicMin(&ctl->u64[4 + f], (unsigned long long)d);
+        if ((long long)d >= T) atomicMin(cu(kCFarMin + f), (unsigned long long)d);
       }
       if (!grid_sync(ctl, a.timeout_ns)) return;
-      const unsigned long long mfar = ld_relaxed(&ctl->u64[4 + f]);
+      const unsigned long long mfar = ld_relaxed(cu(kCFarMin + f));
       const long long T_old = T;
       if (mfar != ~0ull) T = ((long long)mfar > T ? (long long)mfar : T) + delta;
       else T = T + delta;
       // the next near queue holds distances in [T_old, T): its minimum is mfar
       mq = mfar != ~0ull ? (int)mfar : kInf;
-      int* qsize = &ctl->i32[it % 3];
-      int* fsize_next = &ctl->i32[6 + (epoch + 1) % 3];
+      int* qsize = ci(kCQueue + it % 3);
+      int* fsize_next = ci(kCFar + (epoch + 1) % 3);
       for (long long base = gtid & ~31LL; base < fsz; base += gthreads) {
         const long long i = base + lane;
         bool to_near = false, to_far = false;
