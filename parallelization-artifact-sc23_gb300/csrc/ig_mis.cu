@@ -20,7 +20,12 @@
 //   - the undecided vertices are compacted into a worklist each round
 //     (warp-aggregated append), so later rounds touch only what is left;
 //   - vertices with more than 32 neighbours are scanned 32 at a time by the
-//     whole warp with ballots.
+//     whole warp with ballots;
+//   - warps take groups of 32-entry chunks from a per-round counter (the
+//     first group by warp index), so a run of high-degree vertices in
+//     consecutive ids (degree-ordered input) does not sit on a few warps; a
+//     group is up to 8 chunks, sized so every warp takes about 8 groups (few
+//     atomics on a long worklist).
 // The result equals the reference C++ CopyDeterm set bit for bit.  (The CUDA
 // variants compare priorities as signed int and reach a different set.)
 #include "ig_device.cuh"
@@ -56,6 +61,7 @@ __global__ void __launch_bounds__(kThreads) mis_persistent(MisArgs a) {
   const int lane = lane_id();
   const long long gtid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   const long long gthreads = (long long)gridDim.x * blockDim.x;
+  const long long warp_g = gtid >> 5, nwarps = gthreads >> 5;
 
   for (long long v = gtid; v < a.nodes; v += gthreads) {
     a.status[v] = kUndecided;
@@ -69,81 +75,92 @@ __global__ void __launch_bounds__(kThreads) mis_persistent(MisArgs a) {
   int round = 0;
   while (cur_size > 0) {
     const int slot = round % 3;
-    if (gtid == 0) *hot32(ctl, (round + 1) % 3) = 0;
+    if (gtid == 0) {
+      *hot32(ctl, (round + 1) % 3) = 0;      // worklist size of the next round
+      *hot32(ctl, 3 + (round + 1) % 3) = 0;  // its chunks taken
+    }
     int* wsize = hot32(ctl, slot);
-    for (long long base = gtid & ~31LL; base < cur_size; base += gthreads) {
-      const long long i = base + lane;
-      int v = 0, beg = 0, end = 0;
-      bool live = false;
-      if (i < cur_size) {
-        v = (round == 0) ? (int)i : cur[i];
-        live = load_status(a.status, v) == kUndecided;
-        beg = a.resume[v];
-        end = __ldg(&a.nindex[v + 1]);
-      }
-      const unsigned pv = mis_priority(v);
-      bool blocked = false;
-      // light vertices: sequential scan by the owning lane
-      const bool light = live && (end - beg) <= 32;
-      if (light) {
-        int outcome = kIncluded;
-        int k = beg;
-        for (; k < end; k++) {
-          const int n = __ldg(&a.nlist[k]);
-          if (larger(mis_priority(n), n, pv, v)) {
-            const int s = load_status(a.status, n);
-            if (s == kIncluded) { outcome = kExcluded; break; }
-            if (s == kUndecided) { outcome = kUndecided; break; }
-          }
+    int* grab = hot32(ctl, 3 + slot);
+    const int gch = (int)max(1LL, min(8LL, (long long)cur_size / (nwarps * 256)));  // chunks per group
+    for (long long base0 = warp_g * 32 * gch; base0 < cur_size;) {
+      for (int sc = 0; sc < gch && base0 + 32 * sc < cur_size; sc++) {
+        const long long base = base0 + 32 * sc;
+        const long long i = base + lane;
+        int v = 0, beg = 0, end = 0;
+        bool live = false;
+        if (i < cur_size) {
+          v = (round == 0) ? (int)i : cur[i];
+          live = load_status(a.status, v) == kUndecided;
+          beg = a.resume[v];
+          end = __ldg(&a.nindex[v + 1]);
         }
-        if (outcome == kIncluded) {
-          a.status[v] = kIncluded;
-          for (int q = __ldg(&a.nindex[v]); q < end; q++) a.status[__ldg(&a.nlist[q])] = kExcluded;
-        } else if (outcome == kExcluded) {
-          a.status[v] = kExcluded;
-        } else {
-          a.resume[v] = k;
-          blocked = true;
-        }
-      }
-      // heavy vertices: one at a time, the warp scans 32 neighbours per step
-      unsigned heavy = __ballot_sync(IG_FULL, live && !light);
-      while (heavy) {
-        const int src_lane = __ffs(heavy) - 1;
-        heavy &= heavy - 1;
-        const int hv = __shfl_sync(IG_FULL, v, src_lane);
-        const int hb = __shfl_sync(IG_FULL, beg, src_lane);
-        const int he = __shfl_sync(IG_FULL, end, src_lane);
-        const unsigned ph = mis_priority(hv);
-        int outcome = kIncluded, stop = he;
-        for (int k0 = hb; k0 < he; k0 += 32) {
-          const int k = k0 + lane;
-          bool inc = false, und = false;
-          if (k < he) {
+        const unsigned pv = mis_priority(v);
+        bool blocked = false;
+        // light vertices: sequential scan by the owning lane
+        const bool light = live && (end - beg) <= 32;
+        if (light) {
+          int outcome = kIncluded;
+          int k = beg;
+          for (; k < end; k++) {
             const int n = __ldg(&a.nlist[k]);
-            if (larger(mis_priority(n), n, ph, hv)) {
+            if (larger(mis_priority(n), n, pv, v)) {
               const int s = load_status(a.status, n);
-              inc = s == kIncluded;
-              und = s == kUndecided;
+              if (s == kIncluded) { outcome = kExcluded; break; }
+              if (s == kUndecided) { outcome = kUndecided; break; }
             }
           }
-          const unsigned mi = __ballot_sync(IG_FULL, inc);
-          const unsigned mu = __ballot_sync(IG_FULL, und);
-          if (mi) { outcome = kExcluded; break; }
-          if (mu) { outcome = kUndecided; stop = k0 + __ffs(mu) - 1; break; }
+          if (outcome == kIncluded) {
+            a.status[v] = kIncluded;
+            for (int q = __ldg(&a.nindex[v]); q < end; q++) a.status[__ldg(&a.nlist[q])] = kExcluded;
+          } else if (outcome == kExcluded) {
+            a.status[v] = kExcluded;
+          } else {
+            a.resume[v] = k;
+            blocked = true;
+          }
         }
-        if (outcome == kIncluded) {
-          if (lane == 0) a.status[hv] = kIncluded;
-          const int b0 = __ldg(&a.nindex[hv]);
-          for (int q = b0 + lane; q < he; q += 32) a.status[__ldg(&a.nlist[q])] = kExcluded;
-        } else if (outcome == kExcluded) {
-          if (lane == 0) a.status[hv] = kExcluded;
-        } else {
-          if (lane == 0) a.resume[hv] = stop;
-          if (lane == src_lane) blocked = true;
+        // heavy vertices: one at a time, the warp scans 32 neighbours per step
+        unsigned heavy = __ballot_sync(IG_FULL, live && !light);
+        while (heavy) {
+          const int src_lane = __ffs(heavy) - 1;
+          heavy &= heavy - 1;
+          const int hv = __shfl_sync(IG_FULL, v, src_lane);
+          const int hb = __shfl_sync(IG_FULL, beg, src_lane);
+          const int he = __shfl_sync(IG_FULL, end, src_lane);
+          const unsigned ph = mis_priority(hv);
+          int outcome = kIncluded, stop = he;
+          for (int k0 = hb; k0 < he; k0 += 32) {
+            const int k = k0 + lane;
+            bool inc = false, und = false;
+            if (k < he) {
+              const int n = __ldg(&a.nlist[k]);
+              if (larger(mis_priority(n), n, ph, hv)) {
+                const int s = load_status(a.status, n);
+                inc = s == kIncluded;
+                und = s == kUndecided;
+              }
+            }
+            const unsigned mi = __ballot_sync(IG_FULL, inc);
+            const unsigned mu = __ballot_sync(IG_FULL, und);
+            if (mi) { outcome = kExcluded; break; }
+            if (mu) { outcome = kUndecided; stop = k0 + __ffs(mu) - 1; break; }
+          }
+          if (outcome == kIncluded) {
+            if (lane == 0) a.status[hv] = kIncluded;
+            const int b0 = __ldg(&a.nindex[hv]);
+            for (int q = b0 + lane; q < he; q += 32) a.status[__ldg(&a.nlist[q])] = kExcluded;
+          } else if (outcome == kExcluded) {
+            if (lane == 0) a.status[hv] = kExcluded;
+          } else {
+            if (lane == 0) a.resume[hv] = stop;
+            if (lane == src_lane) blocked = true;
+          }
         }
+        warp_append(blocked, v, nxt, wsize, a.nodes, ctl);
       }
-      warp_append(blocked, v, nxt, wsize, a.nodes, ctl);
+      long long nb = 0;
+      if (lane == 0) nb = nwarps * 32 * gch + atomicAdd(grab, 32 * gch);
+      base0 = __shfl_sync(IG_FULL, nb, 0);
     }
     if (!grid_sync(ctl, a.timeout_ns)) return;
     cur_size = ld_relaxed(wsize);
