@@ -57,6 +57,16 @@ __device__ __forceinline__ void tc_items(int out, int in, int block_chunk, int* 
 
 __device__ __forceinline__ bool before(int du, int u, int dw, int w) { return du < dw || (du == dw && u < w); }
 
+// ctl->i32[1] = 1 unless the ids are in (degree, id) order (degrees
+// non-decreasing in id).  In that order before(u, w) is w > u, so the
+// orientation needs no degree lookups and a sorted list splits into its in
+// part (the prefix below u) and its out part (the suffix above u).
+__global__ void tc_rank_check(const int* __restrict__ nindex, int n, IgCtl* ctl) {
+  for (long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x; v + 1 < n;
+       v += (long long)gridDim.x * blockDim.x)
+    if (__ldg(&nindex[v + 2]) - __ldg(&nindex[v + 1]) < __ldg(&nindex[v + 1]) - __ldg(&nindex[v])) ctl->i32[1] = 1;
+}
+
 __global__ void __launch_bounds__(kThreads) tc_orient_count(const int* __restrict__ nindex,
                                                             const int* __restrict__ nlist, int n, int* out_cnt,
                                                             int* item_cnt, int* item_cnt_b, int* hubs,
@@ -66,6 +76,7 @@ __global__ void __launch_bounds__(kThreads) tc_orient_count(const int* __restric
   const int lane = lane_id(), wib = threadIdx.x >> 5;
   const long long gtid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   const long long gthreads = (long long)gridDim.x * blockDim.x;
+  const bool ranked = ctl->i32[1] == 0;
   for (long long base = gtid & ~31LL; base < n; base += gthreads) {
     const long long v = base + lane;
     int beg = 0, deg = 0;
@@ -86,16 +97,12 @@ __global__ void __launch_bounds__(kThreads) tc_orient_count(const int* __restric
       if (act) {
         const int w = __ldg(&nlist[e]);
         if (w == u || (e > ub && __ldg(&nlist[e - 1]) >= w) || w < 0 || w >= n) bad = true;
-        else {
-          const int dw = __ldg(&nindex[w + 1]) - __ldg(&nindex[w]);
-          if (before(du, u, dw, w)) atomicAdd(&s_cnt[wib][j], 1);
-        }
+        else if (ranked ? w > u : before(du, u, __ldg(&nindex[w + 1]) - __ldg(&nindex[w]), w))
+          atomicAdd(&s_cnt[wib][j], 1);
       }
     });
     __syncwarp();
     if (bad) raise(ctl, IG_ERR_UNSORTED);
-    // ids in (degree, id) order make rank order and id order coincide
-    if (v + 1 < n && __ldg(&nindex[v + 2]) - __ldg(&nindex[v + 1]) < deg) ctl->i32[1] = 1;
     if (v < n && !hub) {
       const int oc = s_cnt[wib][lane];
       out_cnt[v] = oc;
@@ -115,6 +122,7 @@ __global__ void __launch_bounds__(kThreads) tc_orient_fill(const int* __restrict
   __shared__ int s_pos[kWarps][32];
   __shared__ int s_ipos[kWarps][32];
   if (ctl->err) return;
+  const bool ranked = ctl->i32[1] == 0;
   const int lane = lane_id(), wib = threadIdx.x >> 5;
   const long long gtid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   const long long gthreads = (long long)gridDim.x * blockDim.x;
@@ -130,6 +138,27 @@ __global__ void __launch_bounds__(kThreads) tc_orient_fill(const int* __restrict
     }
     __syncwarp();
     const int vv = (int)v;
+    if (ranked) {
+      // sorted list in (degree, id) order: the in part is the prefix below v
+      // (in_list from in_off[v] = nindex[v] - out_off[v]), the out part the
+      // suffix from split = nindex[v + 1] - |N+(v)|; each element goes
+      // straight to its place
+      int oo = 0, split = 0;
+      if (v < n) {
+        oo = out_off[v];
+        split = beg + deg - (out_off[v + 1] - oo);
+      }
+      warp_expand(beg, deg > kOrientHub ? 0 : deg, [&](bool act, int e, int j) {
+        const int ooj = __shfl_sync(IG_FULL, oo, j);
+        const int spj = __shfl_sync(IG_FULL, split, j);
+        if (act) {
+          const int w = __ldg(&nlist[e]);
+          if (e >= spj) out_list[ooj + (e - spj)] = w;
+          else in_list[e - ooj] = w;
+        }
+      });
+      continue;
+    }
     warp_expand(beg, deg > kOrientHub ? 0 : deg, [&](bool act, int e, int j) {
       const int u = __shfl_sync(IG_FULL, vv, j);
       const int du = __shfl_sync(IG_FULL, deg, j);
@@ -167,6 +196,7 @@ __global__ void __launch_bounds__(kThreads) tc_orient_hubs_count(const int* __re
   using namespace ig;
   __shared__ int s_tmp[33];
   const int nh = ctl->i32[0];
+  const bool ranked = ctl->i32[1] == 0;
   for (int h = blockIdx.x; h < nh; h += gridDim.x) {
     const int u = hubs[h];
     const int b = __ldg(&nindex[u]), e = __ldg(&nindex[u + 1]), du = e - b;
@@ -175,7 +205,7 @@ __global__ void __launch_bounds__(kThreads) tc_orient_hubs_count(const int* __re
     for (int k = b + threadIdx.x; k < e; k += blockDim.x) {
       const int w = __ldg(&nlist[k]);
       if (w == u || (k > b && __ldg(&nlist[k - 1]) >= w) || w < 0 || w >= n) bad = true;
-      else if (before(du, u, __ldg(&nindex[w + 1]) - __ldg(&nindex[w]), w)) keep++;
+      else if (ranked ? w > u : before(du, u, __ldg(&nindex[w + 1]) - __ldg(&nindex[w]), w)) keep++;
     }
     if (bad) raise(ctl, IG_ERR_UNSORTED);
     int total;
@@ -197,10 +227,21 @@ __global__ void __launch_bounds__(kThreads) tc_orient_hubs_fill(const int* __res
   __shared__ int s_tmp[33];
   if (ctl->err) return;
   const int nh = ctl->i32[0];
+  const bool ranked = ctl->i32[1] == 0;
   for (int h = blockIdx.x; h < nh; h += gridDim.x) {
     const int u = hubs[h];
     const int b = __ldg(&nindex[u]), e = __ldg(&nindex[u + 1]), du = e - b;
     int op = out_off[u], ip = b - op;
+    if (ranked) {
+      // (degree, id) order: in part = the prefix below u, out part = the suffix
+      const int split = e - (out_off[u + 1] - op);
+      for (int k = b + threadIdx.x; k < e; k += blockDim.x) {
+        const int w = __ldg(&nlist[k]);
+        if (k >= split) out_list[op + (k - split)] = w;
+        else in_list[ip + (k - b)] = w;
+      }
+      continue;
+    }
     for (int t = b; t < e; t += blockDim.x) {
       const int k = t + threadIdx.x;
       int w = 0;
@@ -549,6 +590,7 @@ static int tc_run(IgExec* ex, int nodes, int edges, const int* d_nindex, const i
                           "memset")))
     return rc;
   const int grid = std::max(1, std::min((nodes + kThreads - 1) / kThreads, ex->sms * 8));
+  tc_rank_check<<<grid, kThreads, 0, ex->stream>>>(d_nindex, nodes, ex->d_ctl);
   tc_orient_count<<<grid, kThreads, 0, ex->stream>>>(d_nindex, d_nlist, nodes, (int*)cnt, (int*)icnt, (int*)icnt_b,
                                                       (int*)hubs, block_chunk, ex->d_ctl);
   tc_orient_hubs_count<<<ex->sms * 8, kThreads, 0, ex->stream>>>(d_nindex, d_nlist, nodes, (const int*)hubs,
@@ -585,6 +627,6 @@ static int tc_run(IgExec* ex, int nodes, int edges, const int* d_nindex, const i
                                                              (const int*)inl, (const int*)ioff, (const int*)itemv,
                                                              nodes, d_count, ex->d_ctl, nullptr, 0);
   }
-  ig_count_launches(9);
+  ig_count_launches(10);
   return ig_cuda_check((int)cudaGetLastError(), "tc launch");
 }
