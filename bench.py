@@ -315,7 +315,8 @@ def run_e2e(ig, g, gd, sources, args, dist: Dist):
     back to pinned host memory.  The copies of a step's inputs run on their
     own stream and overlap work that does not read them: the degree-ordered
     graph (TC's input) loads during BFS and SSSP, and the next step's graph
-    loads once MIS, its last reader, has returned (during PageRank and TC).
+    loads during TC (not during PageRank, whose drop-in call uploads its own
+    copy of the graph and would share the host-to-device bandwidth with it).
     Every step still copies all of its inputs inside the timed region."""
     import ctypes
     L = ig.load()
@@ -374,12 +375,12 @@ def run_e2e(ig, g, gd, sources, args, dist: Dist):
             ig.check(L.ig_sssp_vertex(int(s), ctypes.byref(d.c), h_out, ctypes.byref(t)))
         ig.check(L.ig_cc_vertex(ctypes.byref(d.c), h_out, ctypes.byref(t)))
         ig.check(L.ig_mis_vertex(ctypes.byref(d.c), None, h_out, ctypes.byref(t)))
-        if not last:
-            upload_graph()  # next step's graph, overlapping PageRank and TC
         ctypes.memmove(h_scores, init.ctypes.data, 4 * V)
         ig.check(L.ig_pr(ctypes.byref(hc), h_scores, hp["deg"], PR_EPS, PR_MAX_ITER, ctypes.byref(it),
                          ctypes.byref(t)))
         ig.check(L.ig_stream_synchronize(cs))  # the TC graph is resident
+        if not last:
+            upload_graph()  # next step's graph, overlapping TC (MIS was its last reader)
         ig.check(L.ig_tc_vertex(ctypes.byref(cnt), V, ctypes.cast(dd.c.nindex, ctypes.c_void_p),
                                 ctypes.cast(dd.c.nlist, ctypes.c_void_p), ctypes.byref(t)))
 
