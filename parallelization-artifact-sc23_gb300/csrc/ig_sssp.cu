@@ -114,7 +114,7 @@ __global__ void __launch_bounds__(kThreads, 4) sssp_persistent(SsspArgs a) {
     a.stamp[v] = 0;
     a.farflag[v] = 0;
     a.expanded[v] = kInf;
-    a.inmember[v] = 0;
+    if (a.heavy_split) a.inmember[v] = 0;  // read only by the light/heavy split
   }
   if (gtid < kDeltaSamples && a.edges > 0) {
     const long long e = gtid * a.edges / kDeltaSamples;

@@ -198,6 +198,43 @@ def test_bfs_direction_settings(ig, orc, graphs, alpha, beta):
     assert np.array_equal(r["bfs0"], orc.bfs(g, 3))
 
 
+def test_degree_ordered_ids_match_oracle(ig, orc, graphs):
+    """Ids in (degree, id) order: consecutive runs of high-degree vertices
+    (MIS chunk scheduling), the TC orientation without degree lookups and the
+    exact-bitmap count, SSSP and BFS on the same relabelled graph."""
+    g = graphs["rmat14"].degree_ordered()
+    srcs = [0, g.nodes - 1, g.nodes // 2]
+    r = run_all(ig, g, srcs)
+    for k, s in enumerate(srcs):
+        assert np.array_equal(r[f"bfs{k}"], orc.bfs(g, int(s))), f"bfs src {s}"
+        assert np.array_equal(r[f"sssp{k}"], orc.sssp(g, int(s))), f"sssp src {s}"
+    assert np.array_equal(r["cc"], orc.cc(g))
+    assert np.array_equal(r["mis"], orc.mis(g).astype(np.int32))
+    assert r["tc"] == orc.tc(g)
+
+
+@pytest.mark.parametrize("scale,degree", [(0, 16), (1, 16), (64, 0), (8, 1000000)])
+def test_sssp_window_settings(ig, orc, graphs, scale, degree):
+    """The degree window (a queued vertex of degree d is expanded once its
+    distance is below the round minimum + C/d) only reorders work: off, very
+    narrow, applied to every vertex, or to none, the distances are exact."""
+    old = (ig.get_option("sssp_window_scale"), ig.get_option("sssp_window_degree"))
+    try:
+        ig.set_option("sssp_window_scale", scale)
+        ig.set_option("sssp_window_degree", degree)
+        for name in ("rmat14", "hubby", "road128"):
+            g = graphs[name]
+            srcs = [0, g.nodes // 2]
+            with ig.DeviceCSR(g) as d:
+                for s in srcs:
+                    dist = np.empty(g.nodes, np.int32)
+                    ig.GPUsssp_vertex(int(s), d, dist)
+                    assert np.array_equal(dist, orc.sssp(g, int(s))), f"{name} src {s}"
+    finally:
+        ig.set_option("sssp_window_scale", old[0])
+        ig.set_option("sssp_window_degree", old[1])
+
+
 @pytest.mark.parametrize("delta", [1, 7, 1000, 100000000])
 def test_sssp_bucket_widths(ig, orc, graphs, delta):
     g = graphs["road128"]
