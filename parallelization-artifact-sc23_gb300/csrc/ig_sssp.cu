@@ -12,8 +12,9 @@
 //
 // Near phase: the near queue is expanded in chunks of 32 vertices per warp;
 // a vertex with more than warp_degree neighbours instead becomes work items of
-// item_edges edges, expanded after the round's barrier one whole warp per item
-// and taken dynamically, so no warp holds the round up with a long list.  An
+// item_edges edges, expanded after the round's barrier in 128-edge slices,
+// one whole warp per slice, taken dynamically, so no warp holds the round up
+// with a long list.  An
 // improved vertex with distance < T joins the next near queue
 // (once per iteration, by stamp) and otherwise the far pile (once per epoch,
 // by flag).  A queued vertex is expanded only if its distance is below the
@@ -25,7 +26,7 @@
 // so the longer the list, the closer to Dijkstra order it is expanded, while
 // short lists keep the parallelism of expanding everything queued.  When the
 // near queue runs dry the far pile is split: the minimum
-// pending distance m is found, T becomes max(T, m) + delta, entries below the
+// pending distance mf is found, T becomes max(T, mf) + delta, entries below the
 // old T are stale (already settled through the near queue) and dropped,
 // entries below the new T form the next near queue, the rest stay far.
 #include "ig_device.cuh"
