@@ -660,7 +660,7 @@ IgOptions& ig_options() {
       /*sssp_window_degree=*/16,
       /*pr_hub_degree=*/1024,
       /*pr_chunk=*/4096,
-      /*pr_blocks_per_sm=*/3,
+      /*pr_blocks_per_sm=*/4,
       /*tc_block_chunk=*/4096,
   };
   return o;

@@ -36,7 +36,7 @@ AXES = {
              "sssp_window_degree": [16, 64], "sssp_delta_scale": [128, 32], "sssp_heavy_split": [0, 1]},
     "cc": {"blocks_per_sm": [4, 8], "hub_degree": [256, 64, 4096]},
     "mis": {"blocks_per_sm": [4, 2, 8]},
-    "pr": {"pr_blocks_per_sm": [3, 2, 4], "pr_hub_degree": [1024, 256, 4096], "pr_chunk": [4096, 512]},
+    "pr": {"pr_blocks_per_sm": [4, 3, 2], "pr_hub_degree": [1024, 256, 4096], "pr_chunk": [4096, 512]},
     "tc": {"tc_block_chunk": [4096, 1024]},
 }
 # short labels for the variant names (like the suite's style words)
