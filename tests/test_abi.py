@@ -53,6 +53,27 @@ def test_options_roundtrip(ig):
         ig.set_option("blocks_per_sm", 1000)
 
 
+def test_kernel_option_defaults_and_ranges(ig):
+    """The SSSP work-item and degree-window knobs and the PageRank residency
+    have the measured defaults, accept their range and refuse values outside
+    it (the work-item size is capped so a round's slice count stays small)."""
+    defaults = {"sssp_item_edges": 256, "sssp_warp_degree": 64, "sssp_window_scale": 8,
+                "sssp_window_degree": 16, "pr_blocks_per_sm": 4, "tc_block_chunk": 4096}
+    for name, value in defaults.items():
+        assert ig.get_option(name) == value, name
+    for name, ok, bad in [("sssp_item_edges", 4096, 4097), ("sssp_item_edges", 32, 31),
+                          ("sssp_window_scale", 0, -1), ("sssp_window_degree", 0, -1)]:
+        old = ig.get_option(name)
+        try:
+            ig.set_option(name, ok)
+            assert ig.get_option(name) == ok
+            with pytest.raises(ig.IndigoError):
+                ig.set_option(name, bad)
+            assert ig.get_option(name) == ok
+        finally:
+            ig.set_option(name, old)
+
+
 def test_dropins_reject_bad_arguments_without_device(ig):
     L = ig.load()
     t = ctypes.c_double()
