@@ -17,8 +17,10 @@ value = 36 * E / step time.
 `--impl ours` (default) prints one JSON line with the device-resident value,
 the end-to-end value through the reference-facing C ABI with host buffers,
 the roofline of the dominant kernel and the CPU baseline.  `--impl reference`
-times the reference's CPU algorithms (the oracle's threaded restatement of the
-best published C++ variants) on the host cores for the same workload.
+times the reference's own best-published C++ variants (built from its staged
+sources into oracle/_ref; the oracle's threaded restatement of them where
+they are not built) on the host cores for the same workload, every step the
+full workload, and loads no GPU library.
 """
 from __future__ import annotations
 
@@ -257,7 +259,7 @@ def run_ours(args, dist: Dist):
     per["pr"]["iterations"] = pr_iters
     shares = {k: acc[k] / max(1e-9, sum(acc.values())) for k in ALGOS}
     dom = max(shares, key=shares.get)
-    traffic = load_traffic().get(dom)
+    traffic = DRAM_BYTES_PER_CALL.get(dom)
     roofline = {"bound": "hbm", "kernel": dom, "achieved": per[dom]["achieved_gbs"], "peak": peaks["hbm_gbs"],
                 "peak_source": peaks["source"], "unit": "GB/s",
                 "frac": round(per[dom]["achieved_gbs"] / peaks["hbm_gbs"], 4), "traffic": traffic,
@@ -463,79 +465,146 @@ def load_peaks() -> dict:
     return {"hbm_gbs": 6800.0, "source": "fallback 6.8 TB/s"}
 
 
-def load_traffic() -> dict:
-    """Per-launch DRAM bytes (read + write) of each algorithm's dominant kernel
-    from the committed ncu summary profiles/ncu_traffic.txt, when present."""
-    p = ROOT / "profiles" / "ncu_traffic.txt"
-    out = {}
-    if p.exists():
-        for line in p.read_text().splitlines():
-            parts = line.split()
-            if len(parts) >= 2 and not line.startswith("#"):
-                try:
-                    out[parts[0]] = int(float(parts[1]))
-                except ValueError:
-                    pass
-    return out
+# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per call of the
+# dominant algorithm's kernel on this workload, from one ncu capture of that
+# kernel alone on RMAT-21 scaled to RMAT-22 by edges processed; the capture
+# command and the figures are recorded beside the kernel's profile summary.
+# None where no capture of the current kernel exists.
+DRAM_BYTES_PER_CALL = {}
 
 
 # ----------------------------------------------------------------------------- CPU
-def cpu_sample(g, gd, sources, threads):
-    """One bounded sample of the step on the host cores with the oracle's
-    threaded restatement of the best published C++ variants: BFS and SSSP from
-    one source (scaled x16), CC, MIS, PR (eps 1e-6), TC on the degree-ordered graph."""
-    from oracle import oracle as orc
-    s = int(sources[0])
-    t = {}
-    _, t["bfs"] = orc.bfs_threads(g, s, threads)
-    _, t["sssp"] = orc.sssp_threads(g, s, threads)
-    _, t["cc"] = orc.cc_threads(g, threads)
-    _, t["mis"] = orc.mis_threads(g, threads)
-    _, it, t["pr"] = orc.pr_threads(g, threads, PR_EPS, PR_MAX_ITER)
-    tc, t["tc"] = orc.tc_threads(gd, threads)
-    step_s = N_SOURCES * (t["bfs"] + t["sssp"]) + t["cc"] + t["mis"] + t["pr"] + t["tc"]
-    return step_s, t, tc, it
+class CpuArm:
+    """The step on this host's cores, for the reference arm and the CPU
+    baseline.  kind "reference": the reference's own best-published C++
+    variants (oracle/_ref/time_<algo>, compiled with g++ -O3 -pthread from its
+    staged sources, scripts/run_codes.py:105), one program per algorithm
+    holding its graph, each run timed by the variant's own timer; kind
+    "port": the oracle's threaded restatement of the same variants
+    (oracle/indigo_oracle.c) where those programs are not built.  Both use
+    all host threads.  The reference's PageRank stops at its own
+    EPSILON = 1e-4 (include/pr_cpp.h:45, a compile-time constant), so it does
+    fewer iterations than the GPU's 1e-6; the port runs to 1e-6."""
+
+    def __init__(self, g, gd, sources, threads: int):
+        from oracle import oracle as orc
+        self.orc, self.g, self.gd, self.sources, self.threads = orc, g, gd, [int(s) for s in sources], threads
+        self.kind = "reference" if orc.ref_available() else "port"
+        self.timers = {}
+        self.tmp = None
+        if self.kind == "reference":
+            self.tmp = tempfile.mkdtemp(prefix="indigo_cpu_")
+            egr, egr_d = os.path.join(self.tmp, "g.egr"), os.path.join(self.tmp, "gd.egr")
+            g.write_egr(egr)
+            gd.write_egr(egr_d)
+            for a in ALGOS:
+                self.timers[a] = orc.RefTimer(a, egr_d if a == "tc" else egr, threads)
+            for path in (egr, egr_d):
+                os.unlink(path)  # the programs hold their graphs
+        self.checks = {}
+
+    def step(self) -> tuple:
+        """One full step (16 BFS + 16 SSSP + CC + MIS + PR + TC): returns the
+        host wall time of the step and the per-algorithm seconds."""
+        sec = {a: 0.0 for a in ALGOS}
+        w0 = time.perf_counter()
+        if self.kind == "reference":
+            T = self.timers
+            for a in ("bfs", "sssp"):
+                for s in self.sources:
+                    t, c = T[a].run(s)
+                    sec[a] += t
+                    self.checks.setdefault(a, []).append(c)
+            for a in ("cc", "mis", "pr", "tc"):
+                t, c = T[a].run(0)
+                sec[a] += t
+                self.checks[a] = c
+        else:
+            orc, g, T = self.orc, self.g, self.threads
+            for s in self.sources:
+                sec["bfs"] += orc.bfs_threads(g, s, T)[1]
+            for s in self.sources:
+                sec["sssp"] += orc.sssp_threads(g, s, T)[1]
+            sec["cc"] = orc.cc_threads(g, T)[1]
+            sec["mis"] = orc.mis_threads(g, T)[1]
+            _, it, sec["pr"] = orc.pr_threads(g, T, PR_EPS, PR_MAX_ITER)
+            self.checks["tc"], sec["tc"] = orc.tc_threads(self.gd, T)
+        return time.perf_counter() - w0, sec
+
+    def describe(self) -> str:
+        if self.kind == "reference":
+            return ("the reference's best-published C++ variants (BFS/SSSP/CC/MIS *_CPP_V_Topo_Push_*, "
+                    "TC_CPP_V_IntType_Critical_Cyclic, PR_CPP_Pull_FloatType_AtomicAdd_Block_Determin) built from its "
+                    "own sources with g++ -O3 -pthread, %d threads; PageRank to the reference's EPSILON 1e-4" %
+                    self.threads)
+        return ("the oracle's threaded restatement of the reference's best-published C++ variants "
+                "(oracle/indigo_oracle.c), %d threads; the reference's programs are not built here" % self.threads)
+
+    def close(self):
+        for t in self.timers.values():
+            t.close()
+        if self.tmp:
+            os.rmdir(self.tmp)
+            self.tmp = None
 
 
 def cpu_baseline(g, gd, sources, validation):
+    """One full step of the workload on the host cores (no scaling): the
+    value is the step's 36 runs x E over its measured wall time."""
     threads = os.cpu_count() or 1
-    t0 = time.time()
-    step_s, t, tc, it = cpu_sample(g, gd, sources, threads)
-    value = RUNS_PER_STEP * g.edges / step_s / 1e9
-    validation["tc_matches_cpu"] = (tc == validation.get("tc_count"))
-    return {"value": round(value, 4), "unit": UNIT, "cores": threads, "kind": "port",
-            "sample": "one pass of the step with BFS/SSSP from 1 of the 16 sources (x16 in the step time), "
-                      "CC, MIS, PR (%d iterations), TC; oracle/indigo_oracle.c threaded restatement of the "
-                      "best published C++ variants, %.1fs wall" % (it, time.time() - t0),
-            "seconds": {k: round(v, 4) for k, v in t.items()}}
+    arm = CpuArm(g, gd, sources, threads)
+    try:
+        wall, sec = arm.step()
+    finally:
+        arm.close()
+    if "tc" in arm.checks:
+        validation["tc_matches_cpu"] = int(arm.checks["tc"]) == int(validation.get("tc_count", -1))
+    value = RUNS_PER_STEP * g.edges / wall / 1e9
+    return {"value": round(value, 4), "unit": UNIT, "cores": threads, "kind": arm.kind,
+            "sample": "one full step (BFS and SSSP from all 16 sources, CC, MIS, PR, TC on the degree-ordered "
+                      "graph), measured whole: %s; %.1f s wall" % (arm.describe(), wall),
+            "seconds": {k: round(v, 4) for k, v in sec.items()}}
 
 
 def run_reference(args, dist: Dist):
-    import indigo_gb300 as ig  # host-side generators only (no GPU use)
-    g, gd, sources = make_workload(ig)
+    """The CPU implementation on the host cores, on the same workload and
+    metric.  Loads no GPU library: the graph comes from the oracle's copy of
+    the generator (oracle/workload.c, proven identical by
+    tests/test_oracle_workload.py).  Every step is the full workload, timed
+    whole by the host clock."""
+    from oracle import oracle as orc
     threads = os.cpu_count() or 1
-    for _ in range(args.warmup):
-        cpu_sample(g, gd, sources, threads)
-    total = 0.0
-    detail = None
-    for _ in range(args.steps):
-        step_s, t, tc, it = cpu_sample(g, gd, sources, threads)
-        total += step_s
-        detail = t
+    t0 = time.time()
+    g = orc.gen_rmat(SCALE, EDGE_FACTOR, *RMAT_ABC, seed=SEED, maxw=MAXW, permute=True, threads=threads)
+    gd = g.degree_ordered(threads)
+    sources = g.pick_sources(N_SOURCES, seed=SEED)
+    log(f"[bench] RMAT-{SCALE} (oracle generator): V={g.nodes} E={g.edges} in {time.time() - t0:.1f}s")
+    arm = CpuArm(g, gd, sources, threads)
+    try:
+        for _ in range(args.warmup):
+            arm.step()
+        total, acc = 0.0, {a: 0.0 for a in ALGOS}
+        for _ in range(args.steps):
+            wall, sec = arm.step()
+            total += wall
+            for a in ALGOS:
+                acc[a] += sec[a]
+    finally:
+        arm.close()
     ms_per_step = 1e3 * total / args.steps
-    value = RUNS_PER_STEP * g.edges / (total / args.steps) / 1e9
-    sample = ("each step: BFS/SSSP from 1 of the 16 sources (x16 in the step time), CC, MIS, PR, TC on the "
-              "degree-ordered graph; threaded restatement of the best published C++ variants "
-              "(oracle/indigo_oracle.c; the reference's own programs are built for this container's "
-              "architecture only)")
+    value = RUNS_PER_STEP * g.edges * args.steps / total / 1e9
+    calls = {"bfs": N_SOURCES, "sssp": N_SOURCES, "cc": 1, "mis": 1, "pr": 1, "tc": 1}
+    sample = ("every step is the full workload (BFS and SSSP from all 16 sources, CC, MIS, PR, TC on the "
+              "degree-ordered graph), timed whole by the host clock: " + arm.describe())
     return {"impl": "reference", "metric": METRIC, "value": round(value, 4), "unit": UNIT, "n_gpus": dist.world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms_per_step, 3),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32/f32",
             "data": "synthetic",
             "config": {"workload": f"rmat{SCALE}_ef{EDGE_FACTOR}_six_algorithms", "vertices": g.nodes,
                        "edges": g.edges, "sources": N_SOURCES, "pr_epsilon": PR_EPS},
-            "cpu_baseline": {"value": round(value, 4), "unit": UNIT, "cores": threads, "kind": "port",
-                             "sample": sample, "seconds": {k: round(v, 4) for k, v in detail.items()}},
+            "cpu_baseline": {"value": round(value, 4), "unit": UNIT, "cores": threads, "kind": arm.kind,
+                             "sample": sample,
+                             "seconds_per_call": {a: round(acc[a] / args.steps / calls[a], 4) for a in ALGOS}},
             "e2e": {"value": round(value, 4), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
 
 

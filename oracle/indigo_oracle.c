@@ -633,3 +633,66 @@ double or_tc_threads(int n, const int* nindex, const int* nlist, long long* coun
   *count = tc_total;
   return el;
 }
+
+/* or_pr_f64 with the pull sums spread over T threads (vertex blocks).  Each
+ * vertex's sum runs in adjacency order as in or_pr_f64, so with iters > 0
+ * the scores are the same bits; only the residual is summed per thread
+ * first.  For checks at large sizes. */
+typedef struct {
+  int b, e;
+  const int *nindex, *nlist;
+  const double* contrib;
+  double* scores;
+  double base, damp, err;
+} pr64_work_t;
+
+static void* pr64_worker(void* p) {
+  pr64_work_t* w = (pr64_work_t*)p;
+  double le = 0;
+  for (int i = w->b; i < w->e; i++) {
+    double incoming = 0;
+    for (int j = w->nindex[i]; j < w->nindex[i + 1]; j++) incoming += w->contrib[w->nlist[j]];
+    const double nw = w->base + w->damp * incoming;
+    le += fabs(nw - w->scores[i]);
+    w->scores[i] = nw;
+  }
+  w->err = le;
+  return NULL;
+}
+
+int or_pr_f64_threads(int n, const int* nindex, const int* nlist, const int* degree, double* scores, int iters,
+                      double epsilon, int max_iter, double damp, int T, double* residual) {
+  if (T < 1 || T > 256) T = 1;
+  const double base = (1.0 - damp) / (double)n;
+  double* contrib = (double*)malloc((size_t)n * sizeof(double));
+  if (!contrib) return -1;
+  pr64_work_t ws[256];
+  pthread_t th[256];
+  const int limit = iters > 0 ? iters : max_iter;
+  int it = 0;
+  double error = 0;
+  while (it < limit) {
+    it++;
+    for (int i = 0; i < n; i++) contrib[i] = scores[i] / (double)degree[i];
+    for (int t = 0; t < T; t++) {
+      ws[t].b = (int)((long long)t * n / T);
+      ws[t].e = (int)((long long)(t + 1) * n / T);
+      ws[t].nindex = nindex;
+      ws[t].nlist = nlist;
+      ws[t].contrib = contrib;
+      ws[t].scores = scores;
+      ws[t].base = base;
+      ws[t].damp = damp;
+      pthread_create(&th[t], NULL, pr64_worker, &ws[t]);
+    }
+    error = 0;
+    for (int t = 0; t < T; t++) {
+      pthread_join(th[t], NULL);
+      error += ws[t].err;
+    }
+    if (iters <= 0 && error < epsilon) break;
+  }
+  if (residual) *residual = error;
+  free(contrib);
+  return it;
+}

@@ -114,6 +114,8 @@ def build_shims(reference_include: str, verbose: bool = False) -> list:
 
 
 if __name__ == "__main__":
+    # usage: build.py [--force] [reference_include_dir]
     build(force="--force" in sys.argv, verbose=True)
-    ref = os.environ.get("INDIGO_REFERENCE", "/root/reference")
-    build_shims(os.path.join(ref, "include"), verbose=True)
+    inc = [a for a in sys.argv[1:] if not a.startswith("--")]
+    if inc:
+        build_shims(inc[0], verbose=True)

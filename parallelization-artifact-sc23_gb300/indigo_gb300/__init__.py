@@ -7,8 +7,8 @@ the reference entry functions plus the device-resident graph API."""
 from ._lib import CSR, IndigoError, RunInfo, check, load, LIB_PATH  # noqa: F401
 from .graph import (DeviceBuffer, DeviceCSR, Graph, device_count, erdos_renyi, grid2d,  # noqa: F401
                     read_egr, rmat, road)
-from .dropin import (GPUbfs_edge, GPUbfs_vertex, GPUcc_edge, GPUcc_vertex, GPUmis_vertex,  # noqa: F401
-                     GPUsssp_edge, GPUsssp_vertex, GPUtc_vertex, PR_GPU)
+from .dropin import (GPUbfs_edge, GPUbfs_vertex, GPUcc_edge, GPUcc_vertex, GPUmis_edge, GPUmis_vertex,  # noqa: F401
+                     GPUsssp_edge, GPUsssp_vertex, GPUtc_edge, GPUtc_vertex, PR_GPU)
 from .device import (DeviceGraph, Event, create_stream, get_option, kernel_launches, probe_random_gather,  # noqa: F401
                      set_option,  # noqa: F401
                      set_wait_timeout_ms)

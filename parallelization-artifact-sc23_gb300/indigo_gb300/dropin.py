@@ -103,3 +103,25 @@ def GPUcc_edge(d_g: DeviceCSR, label: np.ndarray, sp: np.ndarray) -> float:
     t = ctypes.c_double()
     check(load().ig_cc_edge(ctypes.byref(d_g.c), label.ctypes.data, sp.ctypes.data, ctypes.byref(t)))
     return t.value
+
+
+def GPUmis_edge(d_g: DeviceCSR, d_sp: int, priority: np.ndarray | None, status: np.ndarray) -> float:
+    """include/mis_edge_cuda.h:54 -- d_sp: DEVICE COO source array (the driver
+    uploads it, include/mis_edge_cuda.h:154-161); status[v] = 1 (in) / 2 (out)."""
+    _out(status, d_g.nodes, np.int32)
+    pp = None
+    if priority is not None:
+        _out(priority, d_g.nodes, np.uint32)
+        pp = priority.ctypes.data
+    t = ctypes.c_double()
+    check(load().ig_mis_edge(ctypes.byref(d_g.c), d_sp, pp, status.ctypes.data, ctypes.byref(t)))
+    return t.value
+
+
+def GPUtc_edge(edges: int, d_nindex: int, d_nlist: int, d_sp: int):
+    """include/tc_edge_cuda.h:42 -- device nindex/nlist/sp pointers.
+    Returns (count, seconds)."""
+    cnt = ctypes.c_longlong()
+    t = ctypes.c_double()
+    check(load().ig_tc_edge(ctypes.byref(cnt), edges, d_nindex, d_nlist, d_sp, ctypes.byref(t)))
+    return int(cnt.value), t.value

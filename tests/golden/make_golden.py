@@ -77,7 +77,7 @@ def run_all(name, g, sources, tmp):
 
 def main():
     if not oracle.build_ref():
-        sys.exit("reference tree not available: cannot regenerate golden fixtures")
+        sys.exit("reference sources neither present nor staged: cannot regenerate golden fixtures")
     arrays = {}
     meta = {"graphs": {}, "digest_only": {}}
     with tempfile.TemporaryDirectory() as tmp:

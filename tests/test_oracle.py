@@ -106,12 +106,12 @@ def test_pr_f64_converges(ig, orc):
     assert res < 1e-13 and it < 2000
 
 
-def _reference_tree() -> bool:
+def _reference_sources() -> bool:
     from oracle import oracle
-    return oracle.reference_tree_present()
+    return oracle.stage_ref()
 
 
-@pytest.mark.skipif(not _reference_tree(), reason="reference tree not present")
+@pytest.mark.skipif(not _reference_sources(), reason="reference sources neither present nor staged")
 def test_oracle_against_live_reference_programs(ig, orc):
     assert orc.build_ref()
     g = ig.rmat(11, 16, seed=21, maxw=1000)
@@ -132,3 +132,32 @@ def test_oracle_against_live_reference_programs(ig, orc):
         assert np.array_equal(np.fromfile(out, np.float32), orc.pr_f32(g, 1e-4, 100)[0])
         orc.run_ref("tc", egr, out, 1)
         assert int(np.fromfile(out, np.int64)[0]) == orc.tc(g)
+
+
+@pytest.mark.skipif(not _reference_sources(), reason="reference sources neither present nor staged")
+def test_reference_timing_programs(ig, orc, tmp_path):
+    """The CPU arm's timing programs (the reference's best-published
+    variants) answer requests with results that agree with the oracle."""
+    assert orc.build_ref()
+    g = ig.rmat(11, 16, seed=21, maxw=1000)
+    gd = g.degree_ordered()
+    egr, egr_d = str(tmp_path / "g.egr"), str(tmp_path / "gd.egr")
+    g.write_egr(egr)
+    gd.write_egr(egr_d)
+    srcs = [int(s) for s in g.pick_sources(2, 5)]
+    with orc.RefTimer("bfs", egr, 2) as t:
+        for s in srcs:
+            sec, reached = t.run(s)
+            assert sec >= 0 and reached == int((orc.bfs(g, s) != 2147483647).sum())
+    with orc.RefTimer("sssp", egr, 2) as t:
+        d = orc.sssp(g, srcs[0])
+        assert t.run(srcs[0])[1] == int(d[d != 2147483647].astype(np.int64).sum())
+    with orc.RefTimer("cc", egr, 2) as t:
+        lab = orc.cc(g)
+        assert t.run()[1] == int((lab == np.arange(g.nodes)).sum())
+    with orc.RefTimer("mis", egr, 2) as t:
+        assert t.run()[1] > 0
+    with orc.RefTimer("pr", egr, 2) as t:
+        assert 0 < t.run()[1] <= 1_000_000_000 + 1000
+    with orc.RefTimer("tc", egr_d, 2) as t:
+        assert t.run()[1] == orc.tc(gd)
