@@ -290,11 +290,22 @@ def run_ours(args, dist: Dist):
     cpu = None
     if dist.world == 1 and not args.no_cpu_baseline:
         cpu = cpu_baseline(g, gd, sources, validation)
+        per["pr"].update(pagerank_error(g, scores.to_array(np.float32, V), pr_iters))
 
     for h in (G, GT):
         h.close()
     d.close()
     dd.close()
+    forms = None
+    if not args.no_forms:
+        bt = run_batched(args, dist)
+        sv = run_served(args, dist)
+        forms = {
+            "batched": {k: bt[k] for k in ("metric", "value", "unit", "ms_per_step", "scaling", "config",
+                                           "per_algo_ms", "pr_iterations_per_graph", "plain", "speedup_vs_plain",
+                                           "clocks", "gpu_launches")},
+            "served": {k: sv[k] for k in ("metric", "value", "unit", "config", "per_kind", "clocks")},
+        }
     out = {
         "metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": dist.world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(ms_per_step, 3), "higher_is_better": True,
@@ -306,7 +317,7 @@ def run_ours(args, dist: Dist):
                    "l2": "inputs larger than L2 (nlist+eweight %.0f MB > 129 MB)" % (8 * E / 1e6),
                    "parallelism": "replicas" if dist.world > 1 else "single GPU"},
         "e2e": e2e, "roofline": roofline, "random_access": random_access, "cpu_baseline": cpu, "clocks": clk, "gpu_launches": launches,
-        "per_algo": per, "validation": validation,
+        "per_algo": per, "validation": validation, "forms": forms,
     }
     return out
 
@@ -566,6 +577,23 @@ def cpu_baseline(g, gd, sources, validation):
             "seconds": {k: round(v, 4) for k, v in sec.items()}}
 
 
+def pagerank_error(g, scores: np.ndarray, iters: int) -> dict:
+    """Error of the GPU's FP32 PageRank (the bench's last call) against the
+    FP64 oracle: run for the same iteration count (arithmetic error) and run
+    to an L1 residual below 1e-12 (total error, including the truncation of
+    stopping at the residual PR_EPS).  Relative L1 = sum|x - ref| / sum(ref);
+    max = max|x - ref| / max(ref)."""
+    from oracle import oracle as orc
+    s64 = scores.astype(np.float64)
+    same, _, _ = orc.pr_f64_threads(g, iters=iters)
+    conv, it_conv, res = orc.pr_f64_threads(g)
+    return {"rel_l1_vs_fp64_same_iterations": float("%.3e" % (np.abs(s64 - same).sum() / same.sum())),
+            "max_rel_vs_fp64_same_iterations": float("%.3e" % (np.abs(s64 - same).max() / same.max())),
+            "rel_l1_vs_fp64_converged": float("%.3e" % (np.abs(s64 - conv).sum() / conv.sum())),
+            "max_rel_vs_fp64_converged": float("%.3e" % (np.abs(s64 - conv).max() / conv.max())),
+            "fp64_converged_iterations": int(it_conv), "fp64_converged_residual": float("%.2e" % res)}
+
+
 def run_reference(args, dist: Dist):
     """The CPU implementation on the host cores, on the same workload and
     metric.  Loads no GPU library: the graph comes from the oracle's copy of
@@ -612,7 +640,14 @@ def run_reference(args, dist: Dist):
 BATCH_GRAPHS, BATCH_VMIN, BATCH_VMAX, BATCH_SEED = 4096, 1024, 65536, 13
 
 
-def run_batched(args, dist: Dist):
+class _At:
+    """A device address with the .ptr attribute the device API takes."""
+
+    def __init__(self, ptr: int):
+        self.ptr = ptr
+
+
+def run_batched(args, dist: Dist, graphs: int = BATCH_GRAPHS):
     """Configuration 4: 4096 graphs (vertex counts log-uniform in [1k, 64k],
     even Erdos-Renyi with average degree 8, odd RMAT with edge factor 8,
     weights in [1, 255], seed 13).  One step = CC, BFS from vertex 0, TC and
@@ -620,15 +655,20 @@ def run_batched(args, dist: Dist):
     value = graphs/s over all ranks.  With N ranks the graphs shard with no
     exchange: "weak" gives every rank its own pack of 4096 graphs (seed 13 +
     rank), "strong" gives each rank an edge-balanced contiguous slice of the
-    one pack.  The plain comparison runs the same four algorithms as one
-    drop-in call per graph and algorithm (a sample of the graphs, scaled)."""
+    one pack.
+
+    The plain comparison runs the same four algorithms on EVERY graph as one
+    device-API call per graph and algorithm (each graph resident in HBM with
+    its own handle, results left on the device), timed the same way as the
+    batched calls: CUDA events on the one stream both use, after an untimed
+    pass that sizes every handle's scratch."""
     import indigo_gb300 as ig
 
     ig.check(ig.load().ig_set_device(dist.local))
     t0 = time.time()
     strong = dist.world > 1 and args.batch_split == "strong"
     seed = BATCH_SEED + (0 if strong else dist.rank)
-    u, vptr = ig.gen_batch(BATCH_GRAPHS, BATCH_VMIN, BATCH_VMAX, 8.0, 8, 0.57, 0.19, 0.19, seed, 255)
+    u, vptr = ig.gen_batch(graphs, BATCH_VMIN, BATCH_VMAX, 8.0, 8, 0.57, 0.19, 0.19, seed, 255)
     if strong:
         g0, g1 = ig.split_batch(u, vptr, dist.world)[dist.rank]
         if g1 <= g0:
@@ -697,34 +737,55 @@ def run_batched(args, dist: Dist):
         raise RuntimeError("batched run failed during timing")
     its = d_its.to_array(np.int32, graphs_here)
     pr_its = {"min": int(its.min()), "median": float(np.median(its)), "max": int(its.max())}
+    batch_tc = d_cnt.to_array(np.uint64, graphs_here)
     ms = dist.max(t_a.elapsed_ms(t_b)) / args.steps
     graphs_all = int(dist.sum(graphs_here))
     value = graphs_all / (ms * 1e-3)
 
-    # plain drop-in calls, one per graph and algorithm, on a sample of graphs
-    rng = np.random.default_rng(BATCH_SEED)
-    sample = np.sort(rng.choice(graphs_here, size=min(args.plain_sample, graphs_here), replace=False))
-    plain_s = 0.0
-    for i in sample:
-        g = ig.unpack(u, vptr, int(i))
-        with ig.DeviceCSR(g) as dg:
-            out = np.empty(g.nodes, np.int32)
-            sc = np.full(g.nodes, np.float32(1.0) / np.float32(g.nodes), np.float32)
-            deg = g.degree()
-            ig.check(L.ig_device_synchronize())
-            t1 = time.perf_counter()
-            ig.GPUcc_vertex(dg, out)
-            ig.GPUbfs_vertex(0, dg, out)
-            ig.GPUtc_vertex(g.nodes, dg.nindex_ptr, dg.nlist_ptr)
-            ig.PR_GPU(g, sc, deg, PR_EPS, PR_MAX_ITER)
-            plain_s += time.perf_counter() - t1
-    plain_value = len(sample) / plain_s
+    # plain: one device-API call per graph and algorithm, every graph
+    t1 = time.time()
+    handles, csrs = [], []
+    for i in range(graphs_here):
+        dg = ig.DeviceCSR(ig.unpack(u, vptr, i))
+        G = ig.DeviceGraph(dg)
+        G.set_stream(b.stream)
+        csrs.append(dg)
+        handles.append(G)
+    vmax = int(sizes.max())
+    p_dist, p_lab, p_sc = ig.DeviceBuffer(4 * vmax), ig.DeviceBuffer(4 * vmax), ig.DeviceBuffer(4 * vmax)
+    p_cnt = ig.DeviceBuffer(8 * graphs_here)
+
+    def plain_pass():
+        for i, G in enumerate(handles):
+            G.cc(p_lab)
+            G.bfs(0, p_dist)
+            G.tc(_At(p_cnt.ptr + 8 * i))
+            ig.check(L.ig_memcpy_async(p_sc.ptr, d_init.ptr + 4 * int(vptr[i]), 4 * int(sizes[i]), 3, b.stream))
+            G.pagerank(p_sc, PR_EPS, PR_MAX_ITER)
+
+    plain_pass()  # sizes every handle's scratch
+    b.synchronize()
+    p_a, p_b = ig.Event(), ig.Event()
+    p_a.record(b.stream)
+    plain_pass()
+    p_b.record(b.stream)
+    b.synchronize()
+    if any(G.last_run().status for G in handles):
+        raise RuntimeError("plain per-graph run failed")
+    plain_ms = dist.max(p_a.elapsed_ms(p_b))
+    same_tc = bool(np.array_equal(p_cnt.to_array(np.uint64, graphs_here), batch_tc))
+    plain_value = graphs_all / (plain_ms * 1e-3)
+    log(f"[bench] plain per-graph pass: {plain_ms:.1f} ms ({time.time() - t1:.1f}s with uploads)")
+    for G in handles:
+        G.close()
+    for dg in csrs:
+        dg.close()
     b.close()
     return {"metric": "graphs/s (4096 packed graphs: CC + BFS + TC + PR per graph)", "value": round(value, 1),
             "unit": "graphs/s", "n_gpus": dist.world, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": round(ms, 3), "higher_is_better": True, "scaling": "strong" if strong else "weak",
             "vs_baseline": None, "dtype": "int32/f32", "data": "synthetic",
-            "config": {"workload": "batch4096_er8_rmat8", "graphs": graphs_all, "graphs_per_rank": graphs_here,
+            "config": {"workload": f"batch{graphs}_er8_rmat8", "graphs": graphs_all, "graphs_per_rank": graphs_here,
                        "vertices": V, "edges": u.edges,
                        "parallelism": (f"{dist.world} ranks, " + ("edge-balanced slices of one pack" if strong
                                        else "one pack per rank")) if dist.world > 1 else "single GPU",
@@ -733,22 +794,31 @@ def run_batched(args, dist: Dist):
             "per_algo_ms": {k: round(v / args.steps, 3) for k, v in acc.items()},
             "pr_iterations_per_graph": pr_its,
             "autotuned": tuned,
-            "plain": {"value": round(plain_value, 1), "unit": "graphs/s", "sample_graphs": int(len(sample)),
-                      "api": "drop-in C ABI, one call per graph and algorithm (host wall clock, results to host)"},
+            "plain": {"value": round(plain_value, 1), "unit": "graphs/s", "graphs": graphs_here,
+                      "ms": round(plain_ms, 3), "tc_counts_equal_batched": same_tc,
+                      "api": "device API (ig_cc, ig_bfs, ig_tc, ig_pagerank), one call per graph and algorithm on "
+                             "every graph, results on the device, CUDA events on the same stream"},
             "speedup_vs_plain": round(value / plain_value, 1), "clocks": clk, "gpu_launches": launches}
 
 
 # ----------------------------------------------------------------------------- served form
 SERVE_SCALE, SERVE_SEED = 24, 17
-SERVE_RATES = [1000, 3000, 10000, 30000, 100000]
+# offered rates (queries/s) per kind: below saturation, then the lowest rate
+# of the configuration's 1k-100k sweep, which saturates both engines (every
+# higher rate only lengthens the queue)
+SERVE_RATES = {"bfs": [50, 100, 200, 1000], "sssp": [10, 20, 40, 1000]}
+SERVE_CAP = {"bfs": 600, "sssp": 300}
 
 
 def run_served(args, dist: Dist):
     """Configuration 5: resident RMAT-24 (seed 17, weights [1, 1000]); Poisson
     arrivals of single-source BFS and SSSP queries (sources uniform over
-    vertices with degree > 0, 4 random targets each) at each offered rate;
-    each query's latency runs from submission to its answer on the host.
-    The plain comparison answers queries one at a time with the drop-in calls."""
+    vertices with degree > 0, 4 random targets each) at each offered rate for
+    about --serve-seconds; a query's latency runs from its submission to its
+    answer on the host.  Below saturation p50/p99 are service latency; at
+    1000/s they include the queue.  The plain comparison answers queries one
+    at a time with the drop-in calls (distances copied to the host and
+    summarised there), timed the same way, from call to summary."""
     import threading
 
     import indigo_gb300 as ig
@@ -758,20 +828,20 @@ def run_served(args, dist: Dist):
     g = ig.rmat(args.serve_scale, 16, 0.57, 0.19, 0.19, seed=SERVE_SEED, maxw=1000)
     log(f"[bench] served graph RMAT-{args.serve_scale}: V={g.nodes} E={g.edges} in {time.time() - t0:.1f}s")
     d = ig.DeviceCSR(g)
-    rng = np.random.default_rng(SERVE_SEED)
+    rng = np.random.default_rng(SERVE_SEED + dist.rank)
     pool = g.pick_sources(4096, seed=SERVE_SEED)
     srv = ig.Server(d, max_pending=1 << 16)
-    # warm-up: one of each
-    for k in (0, 1):
+    for k in (0, 1):  # warm-up: one of each
         srv.wait(srv.submit(k, int(pool[0])), 600000)
     per_kind = {}
     clocks = ClockSampler(dist.local)
     for kind, name in ((0, "bfs"), (1, "sssp")):
         rows = []
-        for rate in SERVE_RATES:
-            n = int(min(args.serve_queries, max(64, rate * args.serve_seconds)))
+        for rate in SERVE_RATES[name]:
+            n = int(min(SERVE_CAP[name], max(30, rate * args.serve_seconds)))
             gaps = rng.exponential(1.0 / rate, n)
             srcs = rng.choice(pool, n)
+            tgts = rng.integers(0, g.nodes, (n, 4))
             tickets = [None] * n
             rejected = [0]
 
@@ -785,7 +855,7 @@ def run_served(args, dist: Dist):
                             break
                         if t_next - now > 2e-4:
                             time.sleep(t_next - now - 1e-4)
-                    t = srv.try_submit(kind, int(srcs[i]), rng.integers(0, g.nodes, 4))
+                    t = srv.try_submit(kind, int(srcs[i]), tgts[i])
                     if t is None:
                         rejected[0] += 1
                     tickets[i] = t
@@ -794,20 +864,14 @@ def run_served(args, dist: Dist):
             w0 = time.perf_counter()
             th.start()
             th.join()
-            lat = []
-            last_done = 0.0
-            first_submit = None
-            for t in tickets:
-                if t is None:
-                    continue
-                a = srv.wait(t, 600000)
-                lat.append(a.latency_s)
+            lat = [srv.wait(t, 600000).latency_s for t in tickets if t is not None]
             wall = time.perf_counter() - w0
             lat = np.array(lat) if lat else np.array([float("nan")])
             rows.append({"offered_qps": rate, "queries": n, "rejected": rejected[0],
                          "achieved_qps": round(len(lat) / wall, 1),
                          "p50_ms": round(1e3 * float(np.percentile(lat, 50)), 3),
-                         "p99_ms": round(1e3 * float(np.percentile(lat, 99)), 3)})
+                         "p99_ms": round(1e3 * float(np.percentile(lat, 99)), 3),
+                         "saturated": bool(len(lat) / wall < 0.9 * rate)})
             log(f"[bench] served {name} @ {rate}/s: {rows[-1]}")
         # plain: one drop-in call per query, one after another
         m = args.plain_queries
@@ -821,23 +885,25 @@ def run_served(args, dist: Dist):
             ig.summarize(kind, int(pool[2 + i]), out, [0, 1, 2, 3])
             ptimes.append(time.perf_counter() - t1)
         ptimes = np.array(ptimes)
-        best = max(rows, key=lambda r: r["achieved_qps"])
-        per_kind[name] = {"rates": rows, "best_achieved_qps": best["achieved_qps"],
+        sat = rows[-1]
+        below = [r for r in rows if not r["saturated"]]
+        per_kind[name] = {"rates": rows, "saturation_qps": sat["achieved_qps"],
+                          "p99_ms_below_saturation": max((r["p99_ms"] for r in below), default=None),
                           "plain_qps": round(1.0 / float(ptimes.mean()), 1),
                           "plain_p50_ms": round(1e3 * float(np.percentile(ptimes, 50)), 3),
                           "plain_p99_ms": round(1e3 * float(np.percentile(ptimes, 99)), 3),
-                          "speedup_vs_plain": round(best["achieved_qps"] * float(ptimes.mean()), 1)}
+                          "speedup_vs_plain": round(sat["achieved_qps"] * float(ptimes.mean()), 1)}
     clk = clocks.stop()
     srv.close()
     d.close()
-    value = dist.sum(sum(v["best_achieved_qps"] for v in per_kind.values()))  # one replica per rank
+    value = dist.sum(sum(v["saturation_qps"] for v in per_kind.values()))  # one replica per rank
     return {"metric": f"served queries/s (RMAT-{args.serve_scale}, BFS and SSSP, Poisson arrivals) with p50/p99 latency",
-            "value": round(value, 1), "unit": "queries/s", "n_gpus": dist.world, "steps": len(SERVE_RATES),
-            "warmup": 1, "ms_per_step": None, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-            "dtype": "int32", "data": "synthetic",
+            "value": round(value, 1), "unit": "queries/s", "n_gpus": dist.world,
+            "steps": sum(len(v) for v in SERVE_RATES.values()), "warmup": 1, "ms_per_step": None,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32", "data": "synthetic",
             "config": {"workload": f"served_rmat{args.serve_scale}", "vertices": g.nodes, "edges": g.edges,
                        "lanes_per_engine": 64, "rates": SERVE_RATES, "targets_per_query": 4,
-                       "l2": "resident graph larger than L2"},
+                       "seconds_per_rate": args.serve_seconds, "l2": "resident graph larger than L2"},
             "per_kind": per_kind, "clocks": clk}
 
 
@@ -856,10 +922,10 @@ def main():
     ap.add_argument("--no-autotune", action="store_true", help="batched form: keep the process-wide options")
     ap.add_argument("--batch-split", choices=["weak", "strong"], default="weak",
                     help="batched form with N ranks: a pack per rank (weak) or slices of one pack (strong)")
-    ap.add_argument("--serve-seconds", type=float, default=1.0, help="offered-load duration per rate")
-    ap.add_argument("--serve-queries", type=int, default=3000, help="cap on queries per rate")
+    ap.add_argument("--serve-seconds", type=float, default=3.0, help="offered-load duration per rate")
+    ap.add_argument("--no-forms", action="store_true",
+                    help="plain form: leave out the batched and served summaries of the default line")
     ap.add_argument("--plain-queries", type=int, default=16)
-    ap.add_argument("--plain-sample", type=int, default=256, help="graphs timed with plain calls (batched form)")
     args = ap.parse_args()
     if args.warmup < 3:
         log("[bench] warm-up raised to 3 (minimum)")

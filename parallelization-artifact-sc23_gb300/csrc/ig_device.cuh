@@ -69,6 +69,18 @@ __device__ __forceinline__ double ld_relaxed(const double* p) {
   return v;
 }
 
+__device__ __forceinline__ void st_relaxed(unsigned long long* p, unsigned long long v) {
+  asm volatile("st.relaxed.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
+__device__ __forceinline__ int ld_acquire(const int* p) {
+  int v;
+  asm volatile("ld.acquire.gpu.global.s32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ void red_add_release(int* p, int v) {
+  asm volatile("red.release.gpu.global.add.s32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
 // Hot counter k of the control block (see IgCtl::hot), as int or 64-bit.
 __device__ __forceinline__ int* hot32(IgCtl* ctl, int k) { return &ctl->hot[k * kCtlSpread]; }
 __device__ __forceinline__ unsigned long long* hot64(IgCtl* ctl, int k) {

@@ -34,7 +34,7 @@ struct IgSync {
 // (queue sizes, work grabs, round minima) sit 256 bytes apart: packed into one
 // line they all queue in one L2 slice, together with the grid barrier's flag
 // that every block polls.
-constexpr int kCtlHot = 24;     // hot counters
+constexpr int kCtlHot = 32;     // hot counters
 constexpr int kCtlSpread = 64;  // ints from one hot counter to the next
 
 struct IgCtl {

@@ -10,7 +10,7 @@
 // control block) lives in one file-scope __device__ array of fixed size,
 // g_bfs_scratch below.  That array is part of the library's device image, so
 // every GPU that loads the library holds it (12 MiB plus the control block,
-// about 7 KB) until exit.
+// about 9 KB) until exit.
 //
 // Limits and rules of use:
 //   * graphs of at most kNoallocMaxNodes (1,048,576) vertices; larger ones are

@@ -12,9 +12,10 @@
 //
 // Near phase: the near queue is expanded in chunks of 32 vertices per warp;
 // a vertex with more than warp_degree neighbours instead becomes work items of
-// item_edges edges, expanded after the round's barrier in 128-edge slices,
-// one whole warp per slice, taken dynamically, so no warp holds the round up
-// with a long list.  An
+// item_edges edges, expanded in 128-edge slices, one whole warp per slice,
+// taken dynamically by the warps that have finished their frontier chunks
+// while the others still add items, so no warp holds the round up with a
+// long list and one grid barrier ends each round.  An
 // improved vertex with distance < T joins the next near queue
 // (once per iteration, by stamp) and otherwise the far pile (once per epoch,
 // by flag).  A queued vertex is expanded only if its distance is below the
@@ -53,16 +54,18 @@ struct SsspArgs {
   int* fb;
   int* stamp;    // near-queue membership stamp
   int* farflag;  // far-pile membership (epoch + 1)
-  int* mlist;     // per-round list of work items: vertex ...
-  int* mchunk;    // ... and which `item_edges`-edge chunk of its list
-  int mcap;       // item capacity
+  // per-round lists of work items, alternating by round: (vertex << 32) |
+  // index of its `item_edges`-edge chunk; kNoItem marks a free slot
+  unsigned long long* items0;
+  unsigned long long* items1;
+  int mcap;       // item capacity of each list
   int* expanded;  // distance each vertex was last expanded with (INT_MAX: never)
   int* members;   // vertices light-expanded since the last heavy pass
   int* inmember;  // 1 while a vertex sits in members
   IgCtl* ctl;
   unsigned long long timeout_ns;
   int item_edges;        // edges per work item
-  int warp_degree;       // vertices with more neighbours than this go to mlist as work items
+  int warp_degree;       // vertices with more neighbours than this become work items
   long long delta;       // > 0: fixed bucket width
   int delta_scale;
   int heavy_split;       // 1: light/heavy edge split (heavy edges relaxed once per bucket)
@@ -82,8 +85,10 @@ enum SsspCounter : int {
   kCMembers = 15,  // [2] member count (light/heavy split), slot mpass % 2
   kCSlices = 17,   // [3] (64-bit) work-item slices taken
   kCFarMin = 20,   // [3] (64-bit) minimum pending distance of epoch f's pile
-  kCCount = 23
+  kCDone = 23,     // [3] warps done with the frontier part of near iteration k
+  kCCount = 26
 };
+constexpr unsigned long long kNoItem = ~0ull;
 static_assert(kCCount <= kCtlHot, "SSSP counters must fit the control block's hot counters");
 // ctl->u64[0..1]   weight-sample sum / count, ctl->u64[2] bucket width
 // ctl->work        relaxations that improved a distance
@@ -122,10 +127,15 @@ __global__ void __launch_bounds__(kThreads, 4) sssp_persistent(SsspArgs a) {
     atomicAdd(&ctl->u64[0], (unsigned long long)max(0, __ldg(&a.eweight[e])));
     atomicAdd(&ctl->u64[1], 1ull);
   }
+  for (long long i = gtid; i < a.mcap; i += gthreads) {
+    a.items0[i] = kNoItem;
+    a.items1[i] = kNoItem;
+  }
   if (gtid == 0) a.qa[0] = a.src;
   if (gtid < kCCount) {
-    if (gtid >= kCSlices) *cu((int)gtid) = gtid >= kCFarMin ? ~0ull : 0ull;
-    else *ci((int)gtid) = (gtid >= kCMin && gtid < kCMin + 3) ? kInf : 0;
+    const int k = (int)gtid;
+    if (k >= kCSlices && k < kCDone) *cu(k) = k >= kCFarMin ? ~0ull : 0ull;  // the 64-bit counters
+    else *ci(k) = (k >= kCMin && k < kCMin + 3) ? kInf : 0;
   }
   if (!grid_sync(ctl, a.timeout_ns)) return;
 
@@ -170,6 +180,7 @@ __global__ void __launch_bounds__(kThreads, 4) sssp_persistent(SsspArgs a) {
         *ci(kCGrab + (it + 1) % 3) = 0;
         *ci(kCItems + (it + 1) % 3) = 0;
         *cu(kCSlices + (it + 1) % 3) = 0;
+        *ci(kCDone + (it + 1) % 3) = 0;
         *ci(kCMin + (it + 2) % 3) = kInf;
         if (heavy) *ci(kCMembers + (mpass + 1) % 2) = 0;
       }
@@ -181,6 +192,15 @@ __global__ void __launch_bounds__(kThreads, 4) sssp_persistent(SsspArgs a) {
       const int far_mark = epoch + 1;
       const int* frontier = heavy ? a.members : cur;
       const int fcount = heavy ? nmem : cur_size;
+      // this round's work items go to list it % 2; the other list held the
+      // previous round's, all consumed before the barrier that began this
+      // round: free its used slots for the next round
+      unsigned long long* items = (it & 1) ? a.items1 : a.items0;
+      {
+        unsigned long long* old_items = (it & 1) ? a.items0 : a.items1;
+        const int nprev = min(ld_relaxed(ci(kCItems + (it + 2) % 3)), a.mcap);
+        for (long long i = gtid; i < nprev; i += gthreads) old_items[i] = kNoItem;
+      }
       // Four edges per lane at a time: their loads, atomics and stamp checks
       // are independent, so they are issued together.  The distance update is
       // a reduction (atomicMin without a result): an edge whose candidate beats
@@ -289,7 +309,9 @@ __global__ void __launch_bounds__(kThreads, 4) sssp_persistent(SsspArgs a) {
         }
         const int itotal = __shfl_sync(IG_FULL, incl, 31);
         int ibase = 0;
-        if (itotal > 0 && lane == 31) ibase = atomicAdd(ci(kCItems + it % 3), itotal);
+        // reserved by lane 0, the lane that later reports the warp done, so
+        // the report orders after the reservation
+        if (itotal > 0 && lane == 0) ibase = atomicAdd(ci(kCItems + it % 3), itotal);
         if (expand) {
           frontier_v++;
           frontier_e += deg;
@@ -304,7 +326,7 @@ __global__ void __launch_bounds__(kThreads, 4) sssp_persistent(SsspArgs a) {
         if (itotal > 0) {
           // the warp writes the chunk's items together: slot idx belongs to
           // the last lane whose exclusive count is <= idx
-          ibase = __shfl_sync(IG_FULL, ibase, 31);
+          ibase = __shfl_sync(IG_FULL, ibase, 0);
           const int excl = incl - cnt;
           for (int i0 = 0; i0 < itotal; i0 += 32) {
             const int idx = i0 + lane;
@@ -317,12 +339,10 @@ __global__ void __launch_bounds__(kThreads, 4) sssp_persistent(SsspArgs a) {
             const int uj = __shfl_sync(IG_FULL, u, j);
             const int c = idx - __shfl_sync(IG_FULL, excl, j);
             if (idx < itotal) {
-              if (ibase + idx < a.mcap) {
-                a.mlist[ibase + idx] = uj;
-                a.mchunk[ibase + idx] = c;
-              } else {
+              if (ibase + idx < a.mcap)
+                st_relaxed(&items[ibase + idx], ((unsigned long long)(unsigned)uj << 32) | (unsigned)c);
+              else
                 raise(ctl, IG_ERR_OVERFLOW);
-              }
             }
           }
         }
@@ -330,38 +350,85 @@ __global__ void __launch_bounds__(kThreads, 4) sssp_persistent(SsspArgs a) {
         if (lane == 0) nb = nwarps * cs + atomicAdd(grab, cs);
         base = __shfl_sync(IG_FULL, nb, 0);
       }
-      warp_buf_flush(nbuf, nbuf_n, nxt, qsize, a.nodes, ctl);
-      warp_buf_flush(fbuf, fbuf_n, far, fsize, a.nodes, ctl);
-      publish_min(nmin, ci(kCMin + (it + 1) % 3));
-      if (!grid_sync(ctl, a.timeout_ns)) return;
-      const int nm = ld_relaxed(ci(kCItems + it % 3));
-      if (nm > 0) {
-        // work items (vertex, chunk of item_edges edges) cut in slices of
-        // kSlice edges, 2^slog slices per item (the last ones of a short
-        // chunk are empty); one whole warp per slice over a contiguous range
-        // (no owner search).  Slices are taken g at a time from a counter
-        // after the first g by warp index, g sized so that every warp takes
-        // several (balance) while a large round needs few atomics; the
-        // vertex's distance is read when its group starts.
+      // Work items (vertex, chunk of item_edges edges), cut in slices of
+      // kSlice edges, 2^slog slices per item (the last ones of a short chunk
+      // are empty); one whole warp per slice over a contiguous range (no
+      // owner search).  A warp done with its frontier chunks reports it and
+      // takes slices while other warps still expand theirs and add items,
+      // so one grid barrier ends the round.  Slices are claimed g at a time
+      // from a counter; a claim beyond the items reserved so far waits for
+      // more items or for every warp's report (then the count is final and
+      // the claim past it is dropped); a reserved item not yet written is
+      // waited for.  Every wait is bounded and watches the error word.
+      __syncwarp();
+      int* done = ci(kCDone + it % 3);
+      if (lane == 0) red_add_release(done, 1);
+      {
         unsigned long long* mgrab = cu(kCSlices + it % 3);
-        const long long units = (long long)nm << slog;
-        const int g = (int)min(8LL, max(1LL, units / (4LL * nwarps)));
-        for (long long j0 = (long long)warp_g * g; j0 < units;) {
-          const long long j1 = min(j0 + g, units);
-          // the group's items (at most g): lane t reads item mfirst + t, so
-          // the headers of the group load together
+        const int* icount = ci(kCItems + it % 3);
+        long long seen = 0;  // slices known to exist (lane 0's view, broadcast)
+        while (true) {
+          long long j0 = 0, j1 = 0;
+          if (lane == 0) {
+            const long long ahead = seen - (long long)ld_relaxed(mgrab);
+            const long long g = min(8LL, max(1LL, ahead / (4LL * nwarps)));
+            j0 = (long long)atomicAdd(mgrab, (unsigned long long)g);
+            j1 = j0 + g;
+            const unsigned long long t0 = globaltimer();
+            unsigned spins = 0;
+            while (true) {
+              const bool fin = ld_acquire(done) == nwarps;  // then every reservation is visible
+              seen = (long long)min(ld_relaxed(icount), a.mcap) << slog;
+              if (fin) {
+                j1 = min(j1, seen);
+                break;
+              }
+              if (j1 <= seen) break;
+              if ((++spins & 15u) == 0 &&
+                  (ld_relaxed(&ctl->err) != 0 || globaltimer() - t0 > a.timeout_ns)) {
+                if (ld_relaxed(&ctl->err) == 0) raise(ctl, IG_ERR_TIMEOUT);
+                j1 = j0;
+                break;
+              }
+              __nanosleep(200);
+            }
+          }
+          j0 = __shfl_sync(IG_FULL, j0, 0);
+          j1 = __shfl_sync(IG_FULL, j1, 0);
+          seen = __shfl_sync(IG_FULL, seen, 0);
+          if (j0 >= j1) break;
+          // the claim's items (at most 8): lane t reads item mfirst + t, so
+          // the headers load together
           const int mfirst = (int)(j0 >> slog);
           const int ni = (int)((j1 - 1) >> slog) - mfirst + 1;
           int hdu = kInf, hb = 0, hd = 0;
+          bool ok = true;
           if (lane < ni) {
-            const int mi = mfirst + lane;
-            const int u = a.mlist[mi];
-            hdu = a.dist[u];
-            const int b0 = __ldg(&a.nindex[u]), d0 = __ldg(&a.nindex[u + 1]) - b0;
-            const int off0 = a.mchunk[mi] * a.item_edges;
-            hb = b0 + off0;
-            hd = min(a.item_edges, d0 - off0);
+            const unsigned long long* slot = &items[mfirst + lane];
+            unsigned long long w = ld_relaxed(slot);
+            if (w == kNoItem) {
+              const unsigned long long t0 = globaltimer();
+              unsigned spins = 0;
+              while ((w = ld_relaxed(slot)) == kNoItem) {
+                if ((++spins & 15u) == 0 &&
+                    (ld_relaxed(&ctl->err) != 0 || globaltimer() - t0 > a.timeout_ns)) {
+                  if (ld_relaxed(&ctl->err) == 0) raise(ctl, IG_ERR_TIMEOUT);
+                  ok = false;
+                  break;
+                }
+                __nanosleep(64);
+              }
+            }
+            if (ok) {
+              const int u = (int)(w >> 32);
+              hdu = a.dist[u];
+              const int b0 = __ldg(&a.nindex[u]), d0 = __ldg(&a.nindex[u + 1]) - b0;
+              const int off0 = (int)(unsigned)w * a.item_edges;
+              hb = b0 + off0;
+              hd = min(a.item_edges, d0 - off0);
+            }
           }
+          if (__ballot_sync(IG_FULL, !ok)) break;
           for (long long j = j0; j < j1; j++) {
             const int t = (int)(j >> slog) - mfirst;
             const int du = __shfl_sync(IG_FULL, hdu, t);
@@ -379,15 +446,12 @@ __global__ void __launch_bounds__(kThreads, 4) sssp_persistent(SsspArgs a) {
             }
             relax4(act, e, duk);
           }
-          unsigned long long nb = 0;
-          if (lane == 0) nb = (unsigned long long)nwarps * g + atomicAdd(mgrab, (unsigned long long)g);
-          j0 = (long long)__shfl_sync(IG_FULL, nb, 0);
         }
-        warp_buf_flush(nbuf, nbuf_n, nxt, qsize, a.nodes, ctl);
-        warp_buf_flush(fbuf, fbuf_n, far, fsize, a.nodes, ctl);
-        publish_min(nmin, ci(kCMin + (it + 1) % 3));
-        if (!grid_sync(ctl, a.timeout_ns)) return;
       }
+      warp_buf_flush(nbuf, nbuf_n, nxt, qsize, a.nodes, ctl);
+      warp_buf_flush(fbuf, fbuf_n, far, fsize, a.nodes, ctl);
+      publish_min(nmin, ci(kCMin + (it + 1) % 3));
+      if (!grid_sync(ctl, a.timeout_ns)) return;
       if (heavy) mpass++;
       cur_size = ld_relaxed(qsize);
       mq = ld_relaxed(ci(kCMin + (it + 1) % 3));
@@ -464,7 +528,7 @@ __global__ void __launch_bounds__(kThreads, 4) sssp_persistent(SsspArgs a) {
 
 int igk_sssp(IgExec* ex, const ig_csr* dg, int src, int* d_dist) {
   const size_t vb = (size_t)dg->nodes * sizeof(int);
-  void *qa, *qb, *fa, *fb, *stamp, *farflag, *mlist, *mchunk;
+  void *qa, *qb, *fa, *fb, *stamp, *farflag, *items0, *items1;
   int rc;
   if ((rc = ig_scratch_get(ex->scratch, IG_SLOT_Q0, vb, &qa))) return rc;
   if ((rc = ig_scratch_get(ex->scratch, IG_SLOT_Q1, vb, &qb))) return rc;
@@ -476,8 +540,10 @@ int igk_sssp(IgExec* ex, const ig_csr* dg, int src, int* d_dist) {
   const IgOptions& op = ig_exec_options(ex);
   const long long mcap_l = (long long)dg->nodes + dg->edges / std::max(1, op.sssp_item_edges) + 1;
   const int mcap = (int)std::min<long long>(mcap_l, 0x7fffffffLL);
-  if ((rc = ig_scratch_get(ex->scratch, IG_SLOT_G0, (size_t)mcap * sizeof(int), &mlist))) return rc;
-  if ((rc = ig_scratch_get(ex->scratch, IG_SLOT_G1, (size_t)mcap * sizeof(int), &mchunk))) return rc;
+  if ((rc = ig_scratch_get(ex->scratch, IG_SLOT_G0, (size_t)mcap * sizeof(unsigned long long), &items0)))
+    return rc;
+  if ((rc = ig_scratch_get(ex->scratch, IG_SLOT_G1, (size_t)mcap * sizeof(unsigned long long), &items1)))
+    return rc;
   void *expanded, *members, *inmember;
   if ((rc = ig_scratch_get(ex->scratch, IG_SLOT_F0, vb, &expanded))) return rc;
   if ((rc = ig_scratch_get(ex->scratch, IG_SLOT_F1, vb, &members))) return rc;
@@ -485,8 +551,8 @@ int igk_sssp(IgExec* ex, const ig_csr* dg, int src, int* d_dist) {
   if ((rc = ig_exec_reset(ex))) return rc;
   const IgOptions& o = ig_exec_options(ex);
   SsspArgs a{dg->nindex, dg->nlist, dg->eweight, dg->nodes, dg->edges, src, d_dist,
-             (int*)qa, (int*)qb, (int*)fa, (int*)fb, (int*)stamp, (int*)farflag, (int*)mlist,
-             (int*)mchunk, mcap,
+             (int*)qa, (int*)qb, (int*)fa, (int*)fb, (int*)stamp, (int*)farflag,
+             (unsigned long long*)items0, (unsigned long long*)items1, mcap,
              (int*)expanded, (int*)members, (int*)inmember, ex->d_ctl, ex->timeout_ns, o.sssp_item_edges,
              o.sssp_warp_degree,
              o.sssp_delta, o.sssp_delta_scale, o.sssp_heavy_split, o.sssp_window_scale,
