@@ -907,6 +907,62 @@ def run_served(args, dist: Dist):
             "per_kind": per_kind, "clocks": clk}
 
 
+# ----------------------------------------------------------------------------- profiling case
+def run_case(args):
+    """One algorithm on one synthetic graph, run --repeat times through the
+    device-resident API: the small, self-contained workload that Nsight
+    Compute captures use (RMAT scale 21 by default: 2,097,152 vertices, about
+    63M directed edges, so the 250 MB neighbour list exceeds the 129 MB L2).
+    Prints one line per run with the CUDA-event time and the algorithmic
+    bytes, so that a capture can be related to the bench's roofline figures.
+
+        python bench.py --case sssp [--scale 21 | --graph road:4096] [--repeat 1] [--opt sssp_delta=100]"""
+    import indigo_gb300 as ig
+    for o in args.opt:
+        name, value = o.split("=")
+        ig.set_option(name, int(value))
+    if args.graph:
+        kind, _, arg = args.graph.partition(":")
+        if kind == "road":  # the high-diameter configuration: 5% of edges deleted, 0.1% shortcuts
+            g = ig.road(int(arg), int(arg), 0.05, 0.001, seed=11, maxw=10000)
+        elif kind == "grid":
+            g = ig.grid2d(int(arg), int(arg), maxw=255)
+        else:
+            g = ig.rmat(int(arg), 16, seed=7, maxw=1000, permute=True)
+    else:
+        g = ig.rmat(args.scale, 16, seed=7, maxw=1000, permute=True)
+    algo = args.case
+    if algo == "tc":
+        g = g.degree_ordered()
+    V, E = g.nodes, g.edges
+    src = int(g.pick_sources(1, seed=7)[0])
+    bytes_per = {"bfs": 4 * (V + 1) + 8 * E + 4 * V, "sssp": 12 * E + 8 * V, "cc": 8 * E + 8 * V,
+                 "mis": 8 * E + 12 * V, "pr": 8 * E + 20 * V, "tc": 8 * E + 4 * V}
+    with ig.DeviceCSR(g) as d:
+        G = ig.DeviceGraph(d)
+        out = ig.DeviceBuffer(4 * V)
+        cnt = ig.DeviceBuffer(8)
+        init = ig.DeviceBuffer.from_array(np.full(V, np.float32(1.0) / np.float32(V), np.float32))
+        a, b = ig.Event(), ig.Event()
+        for r in range(args.repeat):
+            if algo == "pr":
+                ig.check(ig.load().ig_memcpy(out.ptr, init.ptr, 4 * V, 3))
+            a.record(G.stream)
+            {"bfs": lambda: G.bfs(src, out), "sssp": lambda: G.sssp(src, out), "cc": lambda: G.cc(out),
+             "mis": lambda: G.mis(out), "pr": lambda: G.pagerank(out, PR_EPS, PR_MAX_ITER),
+             "tc": lambda: G.tc(cnt)}[algo]()
+            b.record(G.stream)
+            ms = a.elapsed_ms(b)
+            info = G.last_run()
+            ig.check(info.status)
+            mult = max(1, info.iterations) if algo == "pr" else 1
+            gbs = bytes_per[algo] * mult / (ms * 1e-3) / 1e9
+            print(f"{algo} run {r}: {ms:.3f} ms, iterations {info.iterations}, work {info.work}, "
+                  f"aux {list(info.aux)}, {E / (ms * 1e-3) / 1e9:.2f} GTEPS, {gbs:.0f} GB/s algorithmic "
+                  f"(V={V}, E={E})", flush=True)
+        G.close()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -926,7 +982,16 @@ def main():
     ap.add_argument("--no-forms", action="store_true",
                     help="plain form: leave out the batched and served summaries of the default line")
     ap.add_argument("--plain-queries", type=int, default=16)
+    ap.add_argument("--case", choices=ALGOS, default=None,
+                    help="profiling case: run one algorithm --repeat times on --scale/--graph and print each run")
+    ap.add_argument("--scale", type=int, default=21, help="profiling case: RMAT scale")
+    ap.add_argument("--graph", default="", help="profiling case: rmat:<scale> | road:<side> | grid:<side>")
+    ap.add_argument("--repeat", type=int, default=3, help="profiling case: runs")
+    ap.add_argument("--opt", action="append", default=[], help="profiling case: kernel option name=value")
     args = ap.parse_args()
+    if args.case:
+        run_case(args)
+        return
     if args.warmup < 3:
         log("[bench] warm-up raised to 3 (minimum)")
         args.warmup = 3

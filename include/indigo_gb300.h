@@ -219,11 +219,13 @@ int ig_tc_edge(long long* count, int edges, const int* d_nindex, const int* d_nl
  * kernel's scratch is a fixed array inside the library's device image
  * (12 MiB per GPU, held until exit), so graphs are limited to 1,048,576
  * vertices (IG_ERR_INVALID_ARG beyond).  Runs on `stream` (NULL: legacy
- * default) and returns when the result is complete.  No cudaMalloc or
- * cudaFree is made.  The first call on a device resolves the array's address
- * with cudaGetSymbolAddress: make it before any stream capture.  Calls share
- * the array, so calls whose GPU work overlaps race; order them.  Results are
- * identical to ig_bfs_vertex. */
+ * default), reads back a status word and synchronizes `stream` before it
+ * returns.  No cudaMalloc or cudaFree is made.  The first call on a device
+ * resolves the array's address with cudaGetSymbolAddress: make it before any
+ * stream capture.  That address is kept for the process's life, so after
+ * cudaDeviceReset the entry point must not be called on that device again.
+ * Calls share the array, so calls whose GPU work overlaps race; order them.
+ * Errors are reported as by ig_bfs_vertex, whose results it reproduces. */
 int ig_bfs_vertex_noalloc(int src, const ig_csr* d_g, int* d_dist, void* stream);
 
 /* ---------------------------------------------------------------------------

@@ -126,6 +126,8 @@ int ig_exec_reset(IgExec* ex);
 // Synchronises the stream and copies the control block back; returns the
 // device-side status.
 int ig_exec_finish(IgExec* ex);
+// Turns a device-side status word into the call's status and message.
+int ig_device_status(int err);
 unsigned long long ig_timeout_ns();
 
 // Cooperative launch of a persistent kernel with all blocks co-resident.

@@ -22,7 +22,12 @@
 //     array: the caller must order them;
 //   * the first call on each device looks up the array's device address with
 //     cudaGetSymbolAddress (once per device, that device current); make that
-//     first call before any stream capture.
+//     first call before any stream capture.  The address is kept for the
+//     life of the process: after cudaDeviceReset the library's device image
+//     is loaded again and the kept address is no longer valid, so a process
+//     that resets a device must not call this entry point on it afterwards;
+//   * every call copies the device's status word back and synchronizes
+//     `stream` before it returns.
 #include "ig_device.cuh"
 
 namespace {
@@ -87,7 +92,5 @@ extern "C" int ig_bfs_vertex_noalloc(int src, const ig_csr* d_g, int* d_dist, vo
                      "status copy");
   if (!rc) rc = ig_cuda_check((int)cudaStreamSynchronize(ex.stream), "stream synchronize");
   if (rc) return rc;
-  if (err == IG_ERR_TIMEOUT) return ig_fail(err, "a device-side wait timed out");
-  if (err != 0) return ig_fail(err, "device reported status %d", err);
-  return IG_OK;
+  return ig_device_status(err);
 }

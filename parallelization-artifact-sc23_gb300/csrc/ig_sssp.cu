@@ -71,6 +71,7 @@ struct SsspArgs {
   int heavy_split;       // 1: light/heavy edge split (heavy edges relaxed once per bucket)
   int window_scale;      // window constant C = mean weight * window_scale (0: no window)
   int window_degree;     // vertices of at most this degree are never deferred
+  int spin_ns;           // pause between polls of a warp waiting for work items
 };
 
 // Per-round counters: hot counters of the control block (every warp updates
@@ -100,7 +101,8 @@ __device__ __forceinline__ void publish_min(int& v, int* slot) {
   v = ig::kInf;
 }
 
-__global__ void __launch_bounds__(kThreads, 4) sssp_persistent(SsspArgs a) {
+template <bool kMerged, int kMinBlocks>
+__global__ void __launch_bounds__(kThreads, kMinBlocks) sssp_persistent(SsspArgs a) {
   using namespace ig;
   IgCtl* ctl = a.ctl;
   auto ci = [&](int k) { return hot32(ctl, k); };
@@ -127,10 +129,11 @@ __global__ void __launch_bounds__(kThreads, 4) sssp_persistent(SsspArgs a) {
     atomicAdd(&ctl->u64[0], (unsigned long long)max(0, __ldg(&a.eweight[e])));
     atomicAdd(&ctl->u64[1], 1ull);
   }
-  for (long long i = gtid; i < a.mcap; i += gthreads) {
-    a.items0[i] = kNoItem;
-    a.items1[i] = kNoItem;
-  }
+  if (kMerged)
+    for (long long i = gtid; i < a.mcap; i += gthreads) {
+      a.items0[i] = kNoItem;
+      a.items1[i] = kNoItem;
+    }
   if (gtid == 0) a.qa[0] = a.src;
   if (gtid < kCCount) {
     const int k = (int)gtid;
@@ -195,8 +198,8 @@ __global__ void __launch_bounds__(kThreads, 4) sssp_persistent(SsspArgs a) {
       // this round's work items go to list it % 2; the other list held the
       // previous round's, all consumed before the barrier that began this
       // round: free its used slots for the next round
-      unsigned long long* items = (it & 1) ? a.items1 : a.items0;
-      {
+      unsigned long long* items = (kMerged && (it & 1)) ? a.items1 : a.items0;
+      if (kMerged) {
         unsigned long long* old_items = (it & 1) ? a.items0 : a.items1;
         const int nprev = min(ld_relaxed(ci(kCItems + (it + 2) % 3)), a.mcap);
         for (long long i = gtid; i < nprev; i += gthreads) old_items[i] = kNoItem;
@@ -350,16 +353,40 @@ __global__ void __launch_bounds__(kThreads, 4) sssp_persistent(SsspArgs a) {
         if (lane == 0) nb = nwarps * cs + atomicAdd(grab, cs);
         base = __shfl_sync(IG_FULL, nb, 0);
       }
-      // Work items (vertex, chunk of item_edges edges), cut in slices of
+      // Work items (vertex, chunk of item_edges edges) are cut in slices of
       // kSlice edges, 2^slog slices per item (the last ones of a short chunk
-      // are empty); one whole warp per slice over a contiguous range (no
-      // owner search).  A warp done with its frontier chunks reports it and
-      // takes slices while other warps still expand theirs and add items,
-      // so one grid barrier ends the round.  Slices are claimed g at a time
-      // from a counter; a claim beyond the items reserved so far waits for
-      // more items or for every warp's report (then the count is final and
-      // the claim past it is dropped); a reserved item not yet written is
-      // waited for.  Every wait is bounded and watches the error word.
+      // are empty), each expanded by one whole warp over a contiguous range
+      // (no owner search); expand_slices runs slices j0..j1-1 of the items
+      // whose headers lanes 0.. hold (item mfirst + t in lane t).
+      auto expand_slices = [&](long long j0, long long j1, int mfirst, int hdu, int hb, int hd) {
+        for (long long j = j0; j < j1; j++) {
+          const int t = (int)(j >> slog) - mfirst;
+          const int du = __shfl_sync(IG_FULL, hdu, t);
+          const int b = __shfl_sync(IG_FULL, hb, t);
+          const int d = __shfl_sync(IG_FULL, hd, t);
+          const int s0 = (int)(j & ((1LL << slog) - 1)) * kSlice;
+          bool act[4];
+          int e[4], duk[4];
+#pragma unroll
+          for (int k = 0; k < 4; k++) {
+            const int off = s0 + k * 32 + lane;
+            act[k] = off < d;
+            e[k] = b + (act[k] ? off : 0);
+            duk[k] = du;
+          }
+          relax4(act, e, duk);
+        }
+      };
+      // Merged form: a warp done with its frontier chunks reports it and
+      // takes slices while other warps still expand theirs and add items, so
+      // one grid barrier ends the round.  Slices are claimed g at a time from
+      // a counter; a claim beyond the items reserved so far waits for more
+      // items or for every warp's report (then the count is final and the
+      // claim past it is dropped); a reserved item not yet written is waited
+      // for.  Every wait is bounded and watches the error word.  Otherwise the
+      // items are expanded after a barrier, taken the same way.
+      bool end_barrier = true;  // a barrier (after the item pass) ends the round
+      if (kMerged) {
       __syncwarp();
       int* done = ci(kCDone + it % 3);
       if (lane == 0) red_add_release(done, 1);
@@ -370,27 +397,29 @@ __global__ void __launch_bounds__(kThreads, 4) sssp_persistent(SsspArgs a) {
         while (true) {
           long long j0 = 0, j1 = 0;
           if (lane == 0) {
-            const long long ahead = seen - (long long)ld_relaxed(mgrab);
-            const long long g = min(8LL, max(1LL, ahead / (4LL * nwarps)));
-            j0 = (long long)atomicAdd(mgrab, (unsigned long long)g);
-            j1 = j0 + g;
-            const unsigned long long t0 = globaltimer();
-            unsigned spins = 0;
-            while (true) {
-              const bool fin = ld_acquire(done) == nwarps;  // then every reservation is visible
-              seen = (long long)min(ld_relaxed(icount), a.mcap) << slog;
-              if (fin) {
-                j1 = min(j1, seen);
-                break;
+            // claims of 4 slices; the counts are re-read only when the claim
+            // runs past the slices already known to exist
+            j0 = (long long)atomicAdd(mgrab, 4ull);
+            j1 = j0 + 4;
+            if (j1 > seen) {
+              const unsigned long long t0 = globaltimer();
+              unsigned spins = 0;
+              while (true) {
+                const bool fin = ld_acquire(done) == nwarps;  // then every reservation is visible
+                seen = (long long)min(ld_relaxed(icount), a.mcap) << slog;
+                if (fin) {
+                  j1 = min(j1, seen);
+                  break;
+                }
+                if (j1 <= seen) break;
+                if ((++spins & 15u) == 0 &&
+                    (ld_relaxed(&ctl->err) != 0 || globaltimer() - t0 > a.timeout_ns)) {
+                  if (ld_relaxed(&ctl->err) == 0) raise(ctl, IG_ERR_TIMEOUT);
+                  j1 = j0;
+                  break;
+                }
+                __nanosleep(a.spin_ns);
               }
-              if (j1 <= seen) break;
-              if ((++spins & 15u) == 0 &&
-                  (ld_relaxed(&ctl->err) != 0 || globaltimer() - t0 > a.timeout_ns)) {
-                if (ld_relaxed(&ctl->err) == 0) raise(ctl, IG_ERR_TIMEOUT);
-                j1 = j0;
-                break;
-              }
-              __nanosleep(200);
             }
           }
           j0 = __shfl_sync(IG_FULL, j0, 0);
@@ -429,29 +458,48 @@ __global__ void __launch_bounds__(kThreads, 4) sssp_persistent(SsspArgs a) {
             }
           }
           if (__ballot_sync(IG_FULL, !ok)) break;
-          for (long long j = j0; j < j1; j++) {
-            const int t = (int)(j >> slog) - mfirst;
-            const int du = __shfl_sync(IG_FULL, hdu, t);
-            const int b = __shfl_sync(IG_FULL, hb, t);
-            const int d = __shfl_sync(IG_FULL, hd, t);
-            const int s0 = (int)(j & ((1LL << slog) - 1)) * kSlice;
-            bool act[4];
-            int e[4], duk[4];
-#pragma unroll
-            for (int k = 0; k < 4; k++) {
-              const int off = s0 + k * 32 + lane;
-              act[k] = off < d;
-              e[k] = b + (act[k] ? off : 0);
-              duk[k] = du;
+          expand_slices(j0, j1, mfirst, hdu, hb, hd);
+        }
+      }
+      } else {
+        // items expanded after a barrier: every item is written, the count is final
+        warp_buf_flush(nbuf, nbuf_n, nxt, qsize, a.nodes, ctl);
+        warp_buf_flush(fbuf, fbuf_n, far, fsize, a.nodes, ctl);
+        publish_min(nmin, ci(kCMin + (it + 1) % 3));
+        if (!grid_sync(ctl, a.timeout_ns)) return;
+        const int nm = min(ld_relaxed(ci(kCItems + it % 3)), a.mcap);
+        end_barrier = nm > 0;
+        if (nm > 0) {
+          unsigned long long* mgrab = cu(kCSlices + it % 3);
+          const long long units = (long long)nm << slog;
+          const int g = (int)min(8LL, max(1LL, units / (4LL * nwarps)));
+          for (long long j0 = (long long)warp_g * g; j0 < units;) {
+            const long long j1 = min(j0 + g, units);
+            const int mfirst = (int)(j0 >> slog);
+            const int ni = (int)((j1 - 1) >> slog) - mfirst + 1;
+            int hdu = kInf, hb = 0, hd = 0;
+            if (lane < ni) {
+              const unsigned long long w = items[mfirst + lane];
+              const int u = (int)(w >> 32);
+              hdu = a.dist[u];
+              const int b0 = __ldg(&a.nindex[u]), d0 = __ldg(&a.nindex[u + 1]) - b0;
+              const int off0 = (int)(unsigned)w * a.item_edges;
+              hb = b0 + off0;
+              hd = min(a.item_edges, d0 - off0);
             }
-            relax4(act, e, duk);
+            expand_slices(j0, j1, mfirst, hdu, hb, hd);
+            unsigned long long nb = 0;
+            if (lane == 0) nb = (unsigned long long)nwarps * g + atomicAdd(mgrab, (unsigned long long)g);
+            j0 = (long long)__shfl_sync(IG_FULL, nb, 0);
           }
         }
       }
-      warp_buf_flush(nbuf, nbuf_n, nxt, qsize, a.nodes, ctl);
-      warp_buf_flush(fbuf, fbuf_n, far, fsize, a.nodes, ctl);
-      publish_min(nmin, ci(kCMin + (it + 1) % 3));
-      if (!grid_sync(ctl, a.timeout_ns)) return;
+      if (end_barrier) {
+        warp_buf_flush(nbuf, nbuf_n, nxt, qsize, a.nodes, ctl);
+        warp_buf_flush(fbuf, fbuf_n, far, fsize, a.nodes, ctl);
+        publish_min(nmin, ci(kCMin + (it + 1) % 3));
+        if (!grid_sync(ctl, a.timeout_ns)) return;
+      }
       if (heavy) mpass++;
       cur_size = ld_relaxed(qsize);
       mq = ld_relaxed(ci(kCMin + (it + 1) % 3));
@@ -556,7 +604,12 @@ int igk_sssp(IgExec* ex, const ig_csr* dg, int src, int* d_dist) {
              (int*)expanded, (int*)members, (int*)inmember, ex->d_ctl, ex->timeout_ns, o.sssp_item_edges,
              o.sssp_warp_degree,
              o.sssp_delta, o.sssp_delta_scale, o.sssp_heavy_split, o.sssp_window_scale,
-             o.sssp_window_degree};
+             o.sssp_window_degree, o.sssp_spin_ns};
   void* args[] = {&a};
-  return ig_launch_coop(ex, (const void*)sssp_persistent, kThreads, 0, o.blocks_per_sm, args, nullptr);
+  // the register budget follows the residency cap (4, 5 or 6 blocks of 256 threads per SM)
+  const void* kern = o.sssp_merge_items            ? (const void*)sssp_persistent<true, 4>
+                     : o.blocks_per_sm >= 6 || o.blocks_per_sm == 0 ? (const void*)sssp_persistent<false, 6>
+                     : o.blocks_per_sm == 5        ? (const void*)sssp_persistent<false, 5>
+                                                   : (const void*)sssp_persistent<false, 4>;
+  return ig_launch_coop(ex, kern, kThreads, 0, o.blocks_per_sm, args, nullptr);
 }

@@ -1,7 +1,8 @@
 // Drop-in variant for the reference BFS driver include/bfs_vertex_cuda.h: the
 // driver's main() reads the graph, uploads it and calls GPUbfs_vertex three
 // times; this translation unit supplies that entry function from the GB300
-// library.  Build: see INTEGRATION.md.
+// library.  Build: nvcc with the reference's include/ directory and this
+// repository's include/ on the include path, linked against libindigo_gb300.so.
 typedef int basic_t;
 #include "bfs_vertex_cuda.h"
 #include "shim_common.h"

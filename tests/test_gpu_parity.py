@@ -335,3 +335,26 @@ def test_random_gather_probe(ig, gpu):
     assert math.isfinite(rate) and rate > 0
     with pytest.raises(ig.IndigoError):
         ig.probe_random_gather(1 << 33, 1 << 20, 1)
+
+
+@pytest.mark.parametrize("merge,spin", [(1, 0), (1, 1000), (0, 1000)])
+def test_sssp_item_pass_forms(ig, orc, graphs, merge, spin):
+    """Work items expanded in the round that makes them (one grid barrier per
+    round) or after a second barrier: the distances are exact either way."""
+    old = (ig.get_option("sssp_merge_items"), ig.get_option("sssp_spin_ns"), ig.get_option("sssp_warp_degree"))
+    try:
+        ig.set_option("sssp_merge_items", merge)
+        ig.set_option("sssp_spin_ns", spin)
+        for wd in (64, 4):  # 4: almost every list becomes work items
+            ig.set_option("sssp_warp_degree", wd)
+            for name in ("rmat14", "hubby", "road128", "star"):
+                g = graphs[name]
+                with ig.DeviceCSR(g) as d:
+                    for s in (0, g.nodes // 2):
+                        dist = np.empty(g.nodes, np.int32)
+                        ig.GPUsssp_vertex(int(s), d, dist)
+                        assert np.array_equal(dist, orc.sssp(g, int(s))), f"{name} src {s} wd {wd}"
+    finally:
+        ig.set_option("sssp_merge_items", old[0])
+        ig.set_option("sssp_spin_ns", old[1])
+        ig.set_option("sssp_warp_degree", old[2])
