@@ -14,9 +14,9 @@ struct IgOptions {
   int sssp_window_scale;  // SSSP: expansion window C = mean weight * scale (0 = off); a queued vertex
                           // of degree d is expanded once its distance is below round minimum + C / d
   int sssp_window_degree; // SSSP: vertices of at most this degree are never deferred by the window
-  int sssp_merge_items;   // SSSP: 1 = work items taken in the round that makes them (one grid barrier
-                          // per round), 0 = expanded after a second barrier
-  int sssp_spin_ns;       // SSSP: pause between polls of a warp waiting for work items (merged form)
+  int sssp_merge_below;   // SSSP: a round whose frontier is below this expands (up to 65,536 of) its
+                          // work items without a second grid barrier (0 = never)
+  int sssp_spin_ns;       // SSSP: pause between polls of a warp waiting for work items (merged rounds)
   int pr_hub_degree;      // PageRank: degree above which a vertex is split in chunks
   int pr_chunk;           // PageRank: edges per hub chunk
   int pr_blocks_per_sm;   // PageRank: resident blocks per SM (0 = blocks_per_sm)

@@ -54,11 +54,15 @@ struct SsspArgs {
   int* fb;
   int* stamp;    // near-queue membership stamp
   int* farflag;  // far-pile membership (epoch + 1)
-  // per-round lists of work items, alternating by round: (vertex << 32) |
-  // index of its `item_edges`-edge chunk; kNoItem marks a free slot
-  unsigned long long* items0;
-  unsigned long long* items1;
-  int mcap;       // item capacity of each list
+  // work items of a round, (vertex << 32) | index of its `item_edges`-edge
+  // chunk: `items` holds those expanded after the round's barrier; in a
+  // round whose frontier is below merge_below the first kSmallItems go to a
+  // small list (alternating by round, kNoItem marking a free slot) and are
+  // expanded by warps that have finished their frontier chunks
+  unsigned long long* items;
+  unsigned long long* small0;
+  unsigned long long* small1;
+  int mcap;       // item capacity of `items`
   int* expanded;  // distance each vertex was last expanded with (INT_MAX: never)
   int* members;   // vertices light-expanded since the last heavy pass
   int* inmember;  // 1 while a vertex sits in members
@@ -71,6 +75,7 @@ struct SsspArgs {
   int heavy_split;       // 1: light/heavy edge split (heavy edges relaxed once per bucket)
   int window_scale;      // window constant C = mean weight * window_scale (0: no window)
   int window_degree;     // vertices of at most this degree are never deferred
+  int merge_below;       // rounds with a smaller frontier expand their items without a second barrier
   int spin_ns;           // pause between polls of a warp waiting for work items
 };
 
@@ -87,9 +92,11 @@ enum SsspCounter : int {
   kCSlices = 17,   // [3] (64-bit) work-item slices taken
   kCFarMin = 20,   // [3] (64-bit) minimum pending distance of epoch f's pile
   kCDone = 23,     // [3] warps done with the frontier part of near iteration k
-  kCCount = 26
+  kCSlices2 = 26,  // [3] (64-bit) slices taken after the barrier of a merged round
+  kCCount = 29
 };
 constexpr unsigned long long kNoItem = ~0ull;
+constexpr int kSmallItems = 1 << 16;  // items a round expands without a second barrier
 static_assert(kCCount <= kCtlHot, "SSSP counters must fit the control block's hot counters");
 // ctl->u64[0..1]   weight-sample sum / count, ctl->u64[2] bucket width
 // ctl->work        relaxations that improved a distance
@@ -101,7 +108,7 @@ __device__ __forceinline__ void publish_min(int& v, int* slot) {
   v = ig::kInf;
 }
 
-template <bool kMerged, int kMinBlocks>
+template <int kMinBlocks>
 __global__ void __launch_bounds__(kThreads, kMinBlocks) sssp_persistent(SsspArgs a) {
   using namespace ig;
   IgCtl* ctl = a.ctl;
@@ -129,15 +136,15 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) sssp_persistent(SsspArgs
     atomicAdd(&ctl->u64[0], (unsigned long long)max(0, __ldg(&a.eweight[e])));
     atomicAdd(&ctl->u64[1], 1ull);
   }
-  if (kMerged)
-    for (long long i = gtid; i < a.mcap; i += gthreads) {
-      a.items0[i] = kNoItem;
-      a.items1[i] = kNoItem;
-    }
+  for (long long i = gtid; i < kSmallItems; i += gthreads) {
+    a.small0[i] = kNoItem;
+    a.small1[i] = kNoItem;
+  }
   if (gtid == 0) a.qa[0] = a.src;
   if (gtid < kCCount) {
     const int k = (int)gtid;
-    if (k >= kCSlices && k < kCDone) *cu(k) = k >= kCFarMin ? ~0ull : 0ull;  // the 64-bit counters
+    if ((k >= kCSlices && k < kCDone) || k >= kCSlices2)  // the 64-bit counters
+      *cu(k) = (k >= kCFarMin && k < kCDone) ? ~0ull : 0ull;
     else *ci(k) = (k >= kCMin && k < kCMin + 3) ? kInf : 0;
   }
   if (!grid_sync(ctl, a.timeout_ns)) return;
@@ -183,6 +190,7 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) sssp_persistent(SsspArgs
         *ci(kCGrab + (it + 1) % 3) = 0;
         *ci(kCItems + (it + 1) % 3) = 0;
         *cu(kCSlices + (it + 1) % 3) = 0;
+        *cu(kCSlices2 + (it + 1) % 3) = 0;
         *ci(kCDone + (it + 1) % 3) = 0;
         *ci(kCMin + (it + 2) % 3) = kInf;
         if (heavy) *ci(kCMembers + (mpass + 1) % 2) = 0;
@@ -198,11 +206,16 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) sssp_persistent(SsspArgs
       // this round's work items go to list it % 2; the other list held the
       // previous round's, all consumed before the barrier that began this
       // round: free its used slots for the next round
-      unsigned long long* items = (kMerged && (it & 1)) ? a.items1 : a.items0;
-      if (kMerged) {
-        unsigned long long* old_items = (it & 1) ? a.items0 : a.items1;
-        const int nprev = min(ld_relaxed(ci(kCItems + (it + 2) % 3)), a.mcap);
-        for (long long i = gtid; i < nprev; i += gthreads) old_items[i] = kNoItem;
+      // one barrier (merged round) or two; uniform over the grid
+      const bool merged = fcount < a.merge_below;
+      const int nsmall = merged ? kSmallItems : 0;  // items that go to the small list
+      unsigned long long* small = (it & 1) ? a.small1 : a.small0;
+      {
+        // the other small list held the previous round's items, all consumed
+        // before the barrier that began this round: free its used slots
+        unsigned long long* old_small = (it & 1) ? a.small0 : a.small1;
+        const int nprev = min(ld_relaxed(ci(kCItems + (it + 2) % 3)), kSmallItems);
+        for (long long i = gtid; i < nprev; i += gthreads) old_small[i] = kNoItem;
       }
       // Four edges per lane at a time: their loads, atomics and stamp checks
       // are independent, so they are issued together.  The distance update is
@@ -342,8 +355,12 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) sssp_persistent(SsspArgs
             const int uj = __shfl_sync(IG_FULL, u, j);
             const int c = idx - __shfl_sync(IG_FULL, excl, j);
             if (idx < itotal) {
-              if (ibase + idx < a.mcap)
-                st_relaxed(&items[ibase + idx], ((unsigned long long)(unsigned)uj << 32) | (unsigned)c);
+              const unsigned long long w = ((unsigned long long)(unsigned)uj << 32) | (unsigned)c;
+              const int slot = ibase + idx;
+              if (slot < nsmall)
+                st_relaxed(&small[slot], w);
+              else if (slot - nsmall < a.mcap)
+                a.items[slot - nsmall] = w;
               else
                 raise(ctl, IG_ERR_OVERFLOW);
             }
@@ -377,28 +394,57 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) sssp_persistent(SsspArgs
           relax4(act, e, duk);
         }
       };
-      // Merged form: a warp done with its frontier chunks reports it and
-      // takes slices while other warps still expand theirs and add items, so
-      // one grid barrier ends the round.  Slices are claimed g at a time from
-      // a counter; a claim beyond the items reserved so far waits for more
-      // items or for every warp's report (then the count is final and the
-      // claim past it is dropped); a reserved item not yet written is waited
-      // for.  Every wait is bounded and watches the error word.  Otherwise the
-      // items are expanded after a barrier, taken the same way.
-      bool end_barrier = true;  // a barrier (after the item pass) ends the round
-      if (kMerged) {
-      __syncwarp();
-      int* done = ci(kCDone + it % 3);
-      if (lane == 0) red_add_release(done, 1);
-      {
+      // Items expanded after a barrier (every item written, the count final):
+      // g slices at a time, the first g by warp index, the rest taken from
+      // the 64-bit counter `cnt`.
+      auto barrier_items = [&](const unsigned long long* list, int nm, unsigned long long* cnt) {
+        const long long units = (long long)nm << slog;
+        const int g = (int)min(8LL, max(1LL, units / (4LL * nwarps)));
+        for (long long j0 = (long long)warp_g * g; j0 < units;) {
+          const long long j1 = min(j0 + g, units);
+          const int mfirst = (int)(j0 >> slog);
+          const int ni = (int)((j1 - 1) >> slog) - mfirst + 1;
+          int hdu = kInf, hb = 0, hd = 0;
+          if (lane < ni) {
+            const unsigned long long w = list[mfirst + lane];
+            const int u = (int)(w >> 32);
+            hdu = a.dist[u];
+            const int b0 = __ldg(&a.nindex[u]), d0 = __ldg(&a.nindex[u + 1]) - b0;
+            const int off0 = (int)(unsigned)w * a.item_edges;
+            hb = b0 + off0;
+            hd = min(a.item_edges, d0 - off0);
+          }
+          expand_slices(j0, j1, mfirst, hdu, hb, hd);
+          unsigned long long nb = 0;
+          if (lane == 0) nb = (unsigned long long)nwarps * g + atomicAdd(cnt, (unsigned long long)g);
+          j0 = (long long)__shfl_sync(IG_FULL, nb, 0);
+        }
+      };
+      auto end_pass = [&]() {
+        warp_buf_flush(nbuf, nbuf_n, nxt, qsize, a.nodes, ctl);
+        warp_buf_flush(fbuf, fbuf_n, far, fsize, a.nodes, ctl);
+        publish_min(nmin, ci(kCMin + (it + 1) % 3));
+        return grid_sync(ctl, a.timeout_ns);
+      };
+      const int* icount = ci(kCItems + it % 3);
+      bool end_barrier;  // the item pass needs a barrier of its own
+      if (merged) {
+        // A warp done with its frontier chunks reports it and takes slices of
+        // the small list while other warps still expand theirs and add
+        // items.  Slices are claimed 4 at a time from a counter; a claim
+        // beyond the items reserved so far waits for more items or for every
+        // warp's report (then the count is final and the claim past it is
+        // dropped); a reserved item not yet written is waited for.  Every
+        // wait is bounded and watches the error word.  Items beyond the small
+        // list are expanded after the barrier.
+        __syncwarp();
+        int* done = ci(kCDone + it % 3);
+        if (lane == 0) red_add_release(done, 1);
         unsigned long long* mgrab = cu(kCSlices + it % 3);
-        const int* icount = ci(kCItems + it % 3);
         long long seen = 0;  // slices known to exist (lane 0's view, broadcast)
         while (true) {
           long long j0 = 0, j1 = 0;
           if (lane == 0) {
-            // claims of 4 slices; the counts are re-read only when the claim
-            // runs past the slices already known to exist
             j0 = (long long)atomicAdd(mgrab, 4ull);
             j1 = j0 + 4;
             if (j1 > seen) {
@@ -406,7 +452,7 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) sssp_persistent(SsspArgs
               unsigned spins = 0;
               while (true) {
                 const bool fin = ld_acquire(done) == nwarps;  // then every reservation is visible
-                seen = (long long)min(ld_relaxed(icount), a.mcap) << slog;
+                seen = (long long)min(ld_relaxed(icount), kSmallItems) << slog;
                 if (fin) {
                   j1 = min(j1, seen);
                   break;
@@ -426,14 +472,13 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) sssp_persistent(SsspArgs
           j1 = __shfl_sync(IG_FULL, j1, 0);
           seen = __shfl_sync(IG_FULL, seen, 0);
           if (j0 >= j1) break;
-          // the claim's items (at most 8): lane t reads item mfirst + t, so
-          // the headers load together
+          // the claim's items (at most 4): lane t reads item mfirst + t
           const int mfirst = (int)(j0 >> slog);
           const int ni = (int)((j1 - 1) >> slog) - mfirst + 1;
           int hdu = kInf, hb = 0, hd = 0;
           bool ok = true;
           if (lane < ni) {
-            const unsigned long long* slot = &items[mfirst + lane];
+            const unsigned long long* slot = &small[mfirst + lane];
             unsigned long long w = ld_relaxed(slot);
             if (w == kNoItem) {
               const unsigned long long t0 = globaltimer();
@@ -460,46 +505,17 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) sssp_persistent(SsspArgs
           if (__ballot_sync(IG_FULL, !ok)) break;
           expand_slices(j0, j1, mfirst, hdu, hb, hd);
         }
-      }
+        if (!end_pass()) return;
+        const int nbig = min(ld_relaxed(icount) - kSmallItems, a.mcap);
+        end_barrier = nbig > 0;
+        if (nbig > 0) barrier_items(a.items, nbig, cu(kCSlices2 + it % 3));
       } else {
-        // items expanded after a barrier: every item is written, the count is final
-        warp_buf_flush(nbuf, nbuf_n, nxt, qsize, a.nodes, ctl);
-        warp_buf_flush(fbuf, fbuf_n, far, fsize, a.nodes, ctl);
-        publish_min(nmin, ci(kCMin + (it + 1) % 3));
-        if (!grid_sync(ctl, a.timeout_ns)) return;
-        const int nm = min(ld_relaxed(ci(kCItems + it % 3)), a.mcap);
+        if (!end_pass()) return;
+        const int nm = min(ld_relaxed(icount), a.mcap);
         end_barrier = nm > 0;
-        if (nm > 0) {
-          unsigned long long* mgrab = cu(kCSlices + it % 3);
-          const long long units = (long long)nm << slog;
-          const int g = (int)min(8LL, max(1LL, units / (4LL * nwarps)));
-          for (long long j0 = (long long)warp_g * g; j0 < units;) {
-            const long long j1 = min(j0 + g, units);
-            const int mfirst = (int)(j0 >> slog);
-            const int ni = (int)((j1 - 1) >> slog) - mfirst + 1;
-            int hdu = kInf, hb = 0, hd = 0;
-            if (lane < ni) {
-              const unsigned long long w = items[mfirst + lane];
-              const int u = (int)(w >> 32);
-              hdu = a.dist[u];
-              const int b0 = __ldg(&a.nindex[u]), d0 = __ldg(&a.nindex[u + 1]) - b0;
-              const int off0 = (int)(unsigned)w * a.item_edges;
-              hb = b0 + off0;
-              hd = min(a.item_edges, d0 - off0);
-            }
-            expand_slices(j0, j1, mfirst, hdu, hb, hd);
-            unsigned long long nb = 0;
-            if (lane == 0) nb = (unsigned long long)nwarps * g + atomicAdd(mgrab, (unsigned long long)g);
-            j0 = (long long)__shfl_sync(IG_FULL, nb, 0);
-          }
-        }
+        if (nm > 0) barrier_items(a.items, nm, cu(kCSlices + it % 3));
       }
-      if (end_barrier) {
-        warp_buf_flush(nbuf, nbuf_n, nxt, qsize, a.nodes, ctl);
-        warp_buf_flush(fbuf, fbuf_n, far, fsize, a.nodes, ctl);
-        publish_min(nmin, ci(kCMin + (it + 1) % 3));
-        if (!grid_sync(ctl, a.timeout_ns)) return;
-      }
+      if (end_barrier && !end_pass()) return;
       if (heavy) mpass++;
       cur_size = ld_relaxed(qsize);
       mq = ld_relaxed(ci(kCMin + (it + 1) % 3));
@@ -576,7 +592,7 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) sssp_persistent(SsspArgs
 
 int igk_sssp(IgExec* ex, const ig_csr* dg, int src, int* d_dist) {
   const size_t vb = (size_t)dg->nodes * sizeof(int);
-  void *qa, *qb, *fa, *fb, *stamp, *farflag, *items0, *items1;
+  void *qa, *qb, *fa, *fb, *stamp, *farflag, *items, *smalls;
   int rc;
   if ((rc = ig_scratch_get(ex->scratch, IG_SLOT_Q0, vb, &qa))) return rc;
   if ((rc = ig_scratch_get(ex->scratch, IG_SLOT_Q1, vb, &qb))) return rc;
@@ -587,10 +603,11 @@ int igk_sssp(IgExec* ex, const ig_csr* dg, int src, int* d_dist) {
   // items: sum over a round's vertices of ceil(deg / item edges) <= nodes + edges / item edges
   const IgOptions& op = ig_exec_options(ex);
   const long long mcap_l = (long long)dg->nodes + dg->edges / std::max(1, op.sssp_item_edges) + 1;
-  const int mcap = (int)std::min<long long>(mcap_l, 0x7fffffffLL);
-  if ((rc = ig_scratch_get(ex->scratch, IG_SLOT_G0, (size_t)mcap * sizeof(unsigned long long), &items0)))
+  const int mcap = (int)std::min<long long>(mcap_l, 0x7fffffffLL - kSmallItems);
+  if ((rc = ig_scratch_get(ex->scratch, IG_SLOT_G0, (size_t)mcap * sizeof(unsigned long long), &items)))
     return rc;
-  if ((rc = ig_scratch_get(ex->scratch, IG_SLOT_G1, (size_t)mcap * sizeof(unsigned long long), &items1)))
+  if ((rc = ig_scratch_get(ex->scratch, IG_SLOT_G1, 2 * (size_t)kSmallItems * sizeof(unsigned long long),
+                           &smalls)))
     return rc;
   void *expanded, *members, *inmember;
   if ((rc = ig_scratch_get(ex->scratch, IG_SLOT_F0, vb, &expanded))) return rc;
@@ -600,16 +617,16 @@ int igk_sssp(IgExec* ex, const ig_csr* dg, int src, int* d_dist) {
   const IgOptions& o = ig_exec_options(ex);
   SsspArgs a{dg->nindex, dg->nlist, dg->eweight, dg->nodes, dg->edges, src, d_dist,
              (int*)qa, (int*)qb, (int*)fa, (int*)fb, (int*)stamp, (int*)farflag,
-             (unsigned long long*)items0, (unsigned long long*)items1, mcap,
+             (unsigned long long*)items, (unsigned long long*)smalls, (unsigned long long*)smalls + kSmallItems,
+             mcap,
              (int*)expanded, (int*)members, (int*)inmember, ex->d_ctl, ex->timeout_ns, o.sssp_item_edges,
              o.sssp_warp_degree,
              o.sssp_delta, o.sssp_delta_scale, o.sssp_heavy_split, o.sssp_window_scale,
-             o.sssp_window_degree, o.sssp_spin_ns};
+             o.sssp_window_degree, o.sssp_merge_below, o.sssp_spin_ns};
   void* args[] = {&a};
   // the register budget follows the residency cap (4, 5 or 6 blocks of 256 threads per SM)
-  const void* kern = o.sssp_merge_items            ? (const void*)sssp_persistent<true, 4>
-                     : o.blocks_per_sm >= 6 || o.blocks_per_sm == 0 ? (const void*)sssp_persistent<false, 6>
-                     : o.blocks_per_sm == 5        ? (const void*)sssp_persistent<false, 5>
-                                                   : (const void*)sssp_persistent<false, 4>;
+  const void* kern = o.blocks_per_sm >= 6 || o.blocks_per_sm == 0 ? (const void*)sssp_persistent<6>
+                     : o.blocks_per_sm == 5                        ? (const void*)sssp_persistent<5>
+                                                                   : (const void*)sssp_persistent<4>;
   return ig_launch_coop(ex, kern, kThreads, 0, o.blocks_per_sm, args, nullptr);
 }

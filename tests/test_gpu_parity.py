@@ -27,6 +27,7 @@ def graphs(ig, gpu):
     out.update(kat_graphs(ig))
     out["rmat14"] = ig.rmat(14, 16, seed=7, maxw=1000)
     out["road128"] = ig.road(128, 96, 0.05, 0.001, seed=11, maxw=10000)
+    out["rmat18"] = ig.rmat(18, 16, seed=7, maxw=1000)
     return out
 
 
@@ -337,24 +338,29 @@ def test_random_gather_probe(ig, gpu):
         ig.probe_random_gather(1 << 33, 1 << 20, 1)
 
 
-@pytest.mark.parametrize("merge,spin", [(1, 0), (1, 1000), (0, 1000)])
-def test_sssp_item_pass_forms(ig, orc, graphs, merge, spin):
+@pytest.mark.parametrize("merge_below,spin", [(2147483647, 0), (2147483647, 1000), (65536, 1000), (0, 1000)])
+def test_sssp_item_pass_forms(ig, orc, graphs, merge_below, spin):
     """Work items expanded in the round that makes them (one grid barrier per
-    round) or after a second barrier: the distances are exact either way."""
-    old = (ig.get_option("sssp_merge_items"), ig.get_option("sssp_spin_ns"), ig.get_option("sssp_warp_degree"))
+    round) in every round, in rounds below the default frontier size, or
+    after a second barrier in every round: the distances are exact each
+    way.  Degree 4 as the item threshold makes almost every list work items;
+    on RMAT-18 with 32-edge items a merged round holds more than the 65,536
+    items of its small list, so the rest go through the second barrier."""
+    old = {k: ig.get_option(k) for k in ("sssp_merge_below", "sssp_spin_ns", "sssp_warp_degree", "sssp_item_edges")}
     try:
-        ig.set_option("sssp_merge_items", merge)
+        ig.set_option("sssp_merge_below", merge_below)
         ig.set_option("sssp_spin_ns", spin)
-        for wd in (64, 4):  # 4: almost every list becomes work items
+        cases = [(64, 256, n) for n in ("rmat14", "hubby", "road128", "star")] + \
+                [(4, 256, n) for n in ("rmat14", "hubby", "road128", "star")] + [(1, 32, "rmat18")]
+        for wd, ie, name in cases:
             ig.set_option("sssp_warp_degree", wd)
-            for name in ("rmat14", "hubby", "road128", "star"):
-                g = graphs[name]
-                with ig.DeviceCSR(g) as d:
-                    for s in (0, g.nodes // 2):
-                        dist = np.empty(g.nodes, np.int32)
-                        ig.GPUsssp_vertex(int(s), d, dist)
-                        assert np.array_equal(dist, orc.sssp(g, int(s))), f"{name} src {s} wd {wd}"
+            ig.set_option("sssp_item_edges", ie)
+            g = graphs[name]
+            with ig.DeviceCSR(g) as d:
+                for s in (0, g.nodes // 2):
+                    dist = np.empty(g.nodes, np.int32)
+                    ig.GPUsssp_vertex(int(s), d, dist)
+                    assert np.array_equal(dist, orc.sssp(g, int(s))), f"{name} src {s} wd {wd}"
     finally:
-        ig.set_option("sssp_merge_items", old[0])
-        ig.set_option("sssp_spin_ns", old[1])
-        ig.set_option("sssp_warp_degree", old[2])
+        for k, v in old.items():
+            ig.set_option(k, v)
