@@ -332,13 +332,25 @@ typedef struct ig_query_result {
 } ig_query_result;
 /* d_g: device graph (eweight needed for SSSP queries); the graph stays
  * resident and caller-owned.  max_pending bounds the admission queue.
- * Fails with IG_ERR_NOMEM when the engines' state does not fit in free
- * device memory. */
+ * Queries are admitted by device memory: an engine's lane state (BFS: 44
+ * bytes per vertex; SSSP: about 300) is allocated when a query of its kind
+ * is pending and free device memory (less an eighth in reserve) and the
+ * budget below cover it; otherwise the query stays pending (deferred) until
+ * memory frees up -- an idle engine of the other kind is released to make
+ * room.  A query whose engine can never fit completes with status
+ * IG_ERR_NOMEM.  Fails with IG_ERR_NOMEM when even the BFS engine does not
+ * fit in free device memory at creation. */
 int ig_server_create(const ig_csr* d_g, int max_pending, ig_server** out);
 /* kind 0 BFS, 1 SSSP; IG_ERR_BUSY when max_pending queries are waiting. */
 int ig_server_submit(ig_server* s, int kind, int source, const int* targets, int ntargets, long long* ticket);
 int ig_server_wait(ig_server* s, long long ticket, int timeout_ms, ig_query_result* out);
 int ig_server_stats(ig_server* s, long long* completed, long long* steps);
+/* Caps the bytes the engines may hold together (-1: no cap beyond free device
+ * memory); takes effect at the next admission. */
+int ig_server_set_memory_budget(ig_server* s, long long bytes);
+/* Bytes the engines hold now, admissions deferred for lack of memory so far,
+ * engines created so far (a release and a new creation count again). */
+int ig_server_memory(ig_server* s, long long* held_bytes, long long* deferrals, long long* engines_created);
 int ig_server_destroy(ig_server* s);
 
 /* ---------------------------------------------------------------------------

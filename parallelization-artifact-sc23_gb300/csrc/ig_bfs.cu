@@ -43,6 +43,10 @@ struct BfsArgs {
   int beta;
   const int* sources;  // batched form: one source per graph of a disjoint union (else null)
   int nsources;
+  // level bitmaps (three of ceil(nodes / 32) words, by level % 3): the
+  // bottom-up scan tests a neighbour's bit instead of reading its distance.
+  // Null: the scan reads distances (the allocation-free entry point).
+  unsigned* bits;
 };
 
 // Hot counters of the control block, slot s = level % 3: hot32(s) size of the
@@ -57,6 +61,10 @@ __global__ void __launch_bounds__(kThreads) bfs_persistent(BfsArgs a) {
   const long long gthreads = (long long)gridDim.x * blockDim.x;
   const int warp_g = (int)(gtid >> 5);
   const int nwarps = (int)(gthreads >> 5);
+  const long long nwords = ((long long)a.nodes + 31) >> 5;
+  if (a.bits)  // all three level bitmaps start empty but for a single source's bit
+    for (long long i = gtid; i < 3 * nwords; i += gthreads)
+      a.bits[i] = (a.sources == nullptr && i == (a.src >> 5)) ? 1u << (a.src & 31) : 0u;
 
   long long src_deg = 0;
   int cur_size = 1;
@@ -71,6 +79,7 @@ __global__ void __launch_bounds__(kThreads) bfs_persistent(BfsArgs a) {
     for (long long i = gtid; i < a.nsources; i += gthreads) {
       a.dist[a.sources[i]] = 0;
       a.qa[i] = a.sources[i];
+      if (a.bits) atomicOr(&a.bits[a.sources[i] >> 5], 1u << (a.sources[i] & 31));
     }
     cur_size = a.nsources;
     src_deg = a.edges / 2;  // start top-down; the switch rule takes over after level 0
@@ -95,6 +104,14 @@ __global__ void __launch_bounds__(kThreads) bfs_persistent(BfsArgs a) {
     int* nhub = hot32(ctl, 3 + slot);
     unsigned long long* fedges = hot64(ctl, 6 + slot);
     const int next_level = level + 1;
+    // this level's bits (read), the next level's (written; cleared during the
+    // previous level), and the previous level's, cleared now for level + 2
+    const unsigned* cbits = a.bits ? a.bits + (long long)(level % 3) * nwords : nullptr;
+    unsigned* nbits = a.bits ? a.bits + (long long)((level + 1) % 3) * nwords : nullptr;
+    if (a.bits && level > 0) {
+      unsigned* obits = a.bits + (long long)((level + 2) % 3) * nwords;
+      for (long long i = gtid; i < nwords; i += gthreads) obits[i] = 0u;
+    }
 
     if (!bottom_up) {
       auto visit = [&](bool act, int e, int) {
@@ -106,6 +123,7 @@ __global__ void __launch_bounds__(kThreads) bfs_persistent(BfsArgs a) {
           if (a.dist[w] == kInf && atomicCAS(&a.dist[w], kInf, next_level) == kInf) {
             claim = true;
             wdeg = __ldg(&a.nindex[w + 1]) - __ldg(&a.nindex[w]);
+            if (nbits) atomicOr(&nbits[w >> 5], 1u << (w & 31));
           }
         }
         warp_append_w(claim, w, wdeg, nxt, qsize, fedges, a.nodes, ctl);
@@ -136,13 +154,30 @@ __global__ void __launch_bounds__(kThreads) bfs_persistent(BfsArgs a) {
         if (v < a.nodes && a.dist[v] == kInf) {
           const int b = __ldg(&a.nindex[v]), e = __ldg(&a.nindex[v + 1]);
           deg = e - b;
-          for (int k = b; k < e; k++) {
-            if (a.dist[__ldg(&a.nlist[k])] == level) {
-              found = true;
-              break;
+          if (cbits) {
+            // four neighbours per step: their index loads and bit tests are
+            // independent, so they are issued together (plain loads: the bits
+            // were written by this kernel during the previous level)
+            for (int k = b; k < e && !found; k += 4) {
+              int w[4];
+#pragma unroll
+              for (int t = 0; t < 4; t++) w[t] = k + t < e ? __ldg(&a.nlist[k + t]) : -1;
+#pragma unroll
+              for (int t = 0; t < 4; t++) found |= w[t] >= 0 && ((cbits[w[t] >> 5] >> (w[t] & 31)) & 1u);
+            }
+          } else {
+            for (int k = b; k < e; k++) {
+              if (a.dist[__ldg(&a.nlist[k])] == level) {
+                found = true;
+                break;
+              }
             }
           }
           if (found) a.dist[v] = next_level;
+        }
+        if (nbits) {  // the warp's 32 consecutive vertices fill one word of the next bitmap, its only writer
+          const unsigned m = __ballot_sync(IG_FULL, found);
+          if (lane == 0 && (base >> 5) < nwords) nbits[base >> 5] = m;
         }
         warp_append_w(found, (int)v, deg, nxt, qsize, fedges, a.nodes, ctl);
       }
@@ -175,10 +210,13 @@ int igk_bfs(IgExec* ex, const ig_csr* dg, int src, int* d_dist) {
   if ((rc = ig_scratch_get(ex->scratch, IG_SLOT_Q0, vb, &qa))) return rc;
   if ((rc = ig_scratch_get(ex->scratch, IG_SLOT_Q1, vb, &qb))) return rc;
   if ((rc = ig_scratch_get(ex->scratch, IG_SLOT_Q2, vb, &hubs))) return rc;
+  void* bits;
+  if ((rc = ig_scratch_get(ex->scratch, IG_SLOT_V0, 3 * (((size_t)dg->nodes + 31) / 32) * 4, &bits))) return rc;
   if ((rc = ig_exec_reset(ex))) return rc;
   const IgOptions& o = ig_exec_options(ex);
   BfsArgs a{dg->nindex, dg->nlist, dg->nodes, dg->edges, src, d_dist, (int*)qa, (int*)qb, (int*)hubs,
-            ex->d_ctl, ex->timeout_ns, o.hub_degree, o.bfs_alpha, o.bfs_beta, nullptr, 0};
+            ex->d_ctl, ex->timeout_ns, o.hub_degree, o.bfs_alpha, o.bfs_beta, nullptr, 0,
+            o.bfs_bitmap ? (unsigned*)bits : nullptr};
   void* args[] = {&a};
   return ig_launch_coop(ex, (const void*)bfs_persistent, kThreads, 0, o.blocks_per_sm, args, nullptr);
 }
@@ -192,10 +230,13 @@ int igk_bfs_multi(IgExec* ex, const ig_csr* dg, const int* d_sources, int nsourc
   if ((rc = ig_scratch_get(ex->scratch, IG_SLOT_Q0, vb, &qa))) return rc;
   if ((rc = ig_scratch_get(ex->scratch, IG_SLOT_Q1, vb, &qb))) return rc;
   if ((rc = ig_scratch_get(ex->scratch, IG_SLOT_Q2, vb, &hubs))) return rc;
+  void* bits;
+  if ((rc = ig_scratch_get(ex->scratch, IG_SLOT_V0, 3 * (((size_t)dg->nodes + 31) / 32) * 4, &bits))) return rc;
   if ((rc = ig_exec_reset(ex))) return rc;
   const IgOptions& o = ig_exec_options(ex);
   BfsArgs a{dg->nindex, dg->nlist, dg->nodes, dg->edges, 0, d_dist, (int*)qa, (int*)qb, (int*)hubs,
-            ex->d_ctl, ex->timeout_ns, o.hub_degree, o.bfs_alpha, o.bfs_beta, d_sources, nsources};
+            ex->d_ctl, ex->timeout_ns, o.hub_degree, o.bfs_alpha, o.bfs_beta, d_sources, nsources,
+            o.bfs_bitmap ? (unsigned*)bits : nullptr};
   void* args[] = {&a};
   return ig_launch_coop(ex, (const void*)bfs_persistent, kThreads, 0, o.blocks_per_sm, args, nullptr);
 }
@@ -213,7 +254,7 @@ int igk_bfs_launch_prealloc(IgExec* ex, const ig_csr* dg, int src, int* d_dist, 
   if (o.blocks_per_sm > 0) per_sm = std::min(per_sm, o.blocks_per_sm);
   if (per_sm < 1) return ig_fail(IG_ERR_CUDA, "persistent kernel cannot be resident (occupancy 0)");
   BfsArgs a{dg->nindex, dg->nlist, dg->nodes, dg->edges, src, d_dist, qa, qb, hubs,
-            ex->d_ctl, ex->timeout_ns, o.hub_degree, o.bfs_alpha, o.bfs_beta, nullptr, 0};
+            ex->d_ctl, ex->timeout_ns, o.hub_degree, o.bfs_alpha, o.bfs_beta, nullptr, 0, nullptr};
   void* args[] = {&a};
   rc = ig_cuda_check((int)cudaLaunchCooperativeKernel((const void*)bfs_persistent, dim3(per_sm * ex->sms),
                                                       dim3(kThreads), args, 0, ex->stream),

@@ -82,6 +82,39 @@ __global__ void cc_init(const int* __restrict__ nindex, const int* __restrict__ 
   }
 }
 
+// Root of x without writes (for passes where many threads walk the same
+// paths: path-halving writes would make them contend for the same lines).
+__device__ __forceinline__ int find_root_ro(const int* parent, int x) {
+  while (true) {
+    const int p = load_parent(parent, x);
+    if (p == x) return x;
+    x = p;
+  }
+}
+
+// union(v, neighbour r) for every vertex, with read-only root searches; a
+// compression pass follows each round, so the trees stay flat.
+__global__ void cc_link_round(const int* __restrict__ nindex, const int* __restrict__ nlist, int n, int* parent,
+                              int r) {
+  for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < n; v += gridDim.x * blockDim.x) {
+    const int b = __ldg(&nindex[v]), e = __ldg(&nindex[v + 1]);
+    if (b + r >= e) continue;
+    int ru = find_root_ro(parent, v);
+    int rv = find_root_ro(parent, __ldg(&nlist[b + r]));
+    while (ru != rv) {
+      if (ru < rv) {
+        const int t = ru;
+        ru = rv;
+        rv = t;
+      }
+      const int old = atomicCAS(&parent[ru], ru, rv);
+      if (old == ru) break;
+      ru = find_root_ro(parent, old);
+      rv = find_root_ro(parent, rv);
+    }
+  }
+}
+
 __global__ void cc_sample(const int* __restrict__ nindex, const int* __restrict__ nlist, int n, int* parent) {
   for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < n; v += gridDim.x * blockDim.x) {
     const int b = __ldg(&nindex[v]), e = __ldg(&nindex[v + 1]);
@@ -200,7 +233,15 @@ int igk_cc(IgExec* ex, const ig_csr* dg, int* d_label, bool sample) {
   const int grid_v = std::min((n + kThreads - 1) / kThreads, ex->sms * 16);
   const int grid_w = std::max(1, std::min((n + kThreads - 1) / kThreads, ex->sms * 8));
   cc_init<<<grid_v, kThreads, 0, ex->stream>>>(dg->nindex, dg->nlist, n, d_label);
-  if (sample) {
+  if (sample && o.cc_rounds) {
+    // neighbour r of every vertex linked in its own round, trees flattened after each
+    for (int r = 0; r < kSample; r++) {
+      cc_link_round<<<grid_v, kThreads, 0, ex->stream>>>(dg->nindex, dg->nlist, n, d_label, r);
+      cc_compress<<<grid_v, kThreads, 0, ex->stream>>>(d_label, n);
+    }
+    cc_giant<<<1, kThreads, 0, ex->stream>>>(d_label, n, ex->d_ctl);
+    ig_count_launches(2 * kSample + 1);
+  } else if (sample) {
     cc_sample<<<grid_v, kThreads, 0, ex->stream>>>(dg->nindex, dg->nlist, n, d_label);
     cc_compress<<<grid_v, kThreads, 0, ex->stream>>>(d_label, n);
     cc_giant<<<1, kThreads, 0, ex->stream>>>(d_label, n, ex->d_ctl);

@@ -53,6 +53,8 @@ struct PrArgs {
   unsigned long long timeout_ns;
   int hub_degree;
   int chunk;
+  int prefetch;  // 1: each warp prefetches its next vertex group's lists into L2
+  int subwarp;   // 1: medium lists summed four at a time by 8-lane sub-warps (else two by the warp)
   // batched form (disjoint union of graphs): first vertex of each graph,
   // per-graph residuals (3 rotating slots) and per-graph iteration counts
   const int* graph_vptr;
@@ -169,6 +171,53 @@ __device__ __forceinline__ void warp_gather_sum2(const int* __restrict__ nlist, 
   warp_pair_reduce(hi2, lo2);
 }
 
+// Asks L2 to fetch nlist[b, e) ahead of its use (cp.async.bulk.prefetch, 16-byte
+// granules inside the array; no register holds the data, nothing waits on it).
+__device__ __forceinline__ void prefetch_list(const PrArgs& a, int b, int e) {
+  const unsigned long long lo = (unsigned long long)(a.nlist + b) & ~15ull;
+  const unsigned long long end = (unsigned long long)(a.nlist + a.edges) & ~15ull;
+  unsigned long long hi = ((unsigned long long)(a.nlist + e) + 15ull) & ~15ull;
+  if (hi > end) hi = end;
+  if (e > b && hi > lo)
+    asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(lo), "r"((unsigned)(hi - lo)) : "memory");
+}
+
+// Kahan sum of contrib[nlist[k]] over k = b + sub, b + sub + 8, ... < e by
+// the 8 lanes of one sub-warp (sub = lane % 8), returned as a (hi, lo) pair
+// reduced over those lanes (same value in all 8).  Each lane keeps 8 gathers
+// in flight and loads the next 8 indices while the current values arrive.
+// The order depends only on [b, e), so a vertex's sum is the same wherever
+// its list lies.
+__device__ __forceinline__ void subwarp8_gather_sum(const int* __restrict__ nlist, const float* contrib, int b, int e,
+                                                    float& hi, float& lo) {
+  constexpr int kDepth = 8, kW = 8;
+  float s = 0.f, c = 0.f;
+  int k = b + (ig::lane_id() & (kW - 1));
+  int n[kDepth];
+#pragma unroll
+  for (int t = 0; t < kDepth; t++) n[t] = k + kW * t < e ? __ldg(&nlist[k + kW * t]) : 0;
+  while (k < e) {  // lanes of a sub-warp may leave at different steps: no collectives inside
+    float x[kDepth];
+#pragma unroll
+    for (int t = 0; t < kDepth; t++) x[t] = k + kW * t < e ? contrib[n[t]] : 0.f;
+    const int kn = k + kW * kDepth;
+#pragma unroll
+    for (int t = 0; t < kDepth; t++) n[t] = kn + kW * t < e ? __ldg(&nlist[kn + kW * t]) : 0;
+#pragma unroll
+    for (int t = 0; t < kDepth; t++)
+      if (k + kW * t < e) kahan_add(s, c, x[t]);
+    k = kn;
+  }
+  hi = s;
+  lo = -c;
+#pragma unroll
+  for (int o = kW / 2; o > 0; o >>= 1) {
+    const float h2 = __shfl_xor_sync(IG_FULL, hi, o);
+    const float l2 = __shfl_xor_sync(IG_FULL, lo, o);
+    pair_add(hi, lo, h2, l2);
+  }
+}
+
 __device__ __forceinline__ int vdegree(const PrArgs& a, int v) {
   return a.degree ? a.degree[v] : (__ldg(&a.nindex[v + 1]) - __ldg(&a.nindex[v]));
 }
@@ -282,12 +331,29 @@ __global__ void __launch_bounds__(kThreads) pr_persistent(PrArgs a) {
       warp_gather_sum(a.nlist, cur, b, e, shi, slo);
       if (lane == 0) a.partial[c] = make_float2(shi, slo);
     }
+    // each lane's list range of the warp's next group is loaded (and its list
+    // prefetched into L2) while the current group is summed
+    int nb = 0, ne = 0;
+    {
+      const long long v0 = (long long)warp_g * 32 + lane;
+      if (v0 < a.nodes) {
+        nb = __ldg(&a.nindex[v0]);
+        ne = __ldg(&a.nindex[v0 + 1]);
+        if (a.prefetch && ne - nb <= a.hub_degree) prefetch_list(a, nb, ne);
+      }
+    }
     for (long long base = (long long)warp_g * 32; base < a.nodes; base += (long long)nwarps * 32) {
       const long long vi = base + lane;
-      int v = (int)vi, b = 0, e = 0;
-      if (vi < a.nodes) {
-        b = __ldg(&a.nindex[v]);
-        e = __ldg(&a.nindex[v + 1]);
+      int v = (int)vi;
+      const int b = nb, e = ne;
+      {
+        const long long vn = vi + (long long)nwarps * 32;
+        nb = ne = 0;
+        if (vn < a.nodes) {
+          nb = __ldg(&a.nindex[vn]);
+          ne = __ldg(&a.nindex[vn + 1]);
+          if (a.prefetch && ne - nb <= a.hub_degree) prefetch_list(a, nb, ne);
+        }
       }
       int d = e - b;
       float sum = 0.f;
@@ -321,6 +387,27 @@ __global__ void __launch_bounds__(kThreads) pr_persistent(PrArgs a) {
         sum = __fsub_rn(s, c);
       }
       unsigned med = __ballot_sync(IG_FULL, vi < a.nodes && !skip && d > kLight && d <= a.hub_degree);
+      // four medium vertices at a time, one per sub-warp of 8 lanes
+      while (a.subwarp && med) {
+        int o[4];
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+          o[q] = med ? __ffs(med) - 1 : -1;
+          if (med) med &= med - 1;
+        }
+        const int q = lane >> 3;
+        const int mine = q == 0 ? o[0] : q == 1 ? o[1] : q == 2 ? o[2] : o[3];
+        const int mb = __shfl_sync(IG_FULL, b, mine < 0 ? 0 : mine);
+        const int me = __shfl_sync(IG_FULL, e, mine < 0 ? 0 : mine);
+        float h, l;
+        subwarp8_gather_sum(a.nlist, cur, mb, mine < 0 ? mb : me, h, l);
+        const float tot = __fadd_rn(h, l);
+#pragma unroll
+        for (int r = 0; r < 4; r++) {
+          const float t = __shfl_sync(IG_FULL, tot, r * 8);
+          if (lane == o[r]) sum = t;
+        }
+      }
       // two medium vertices at a time, so short ones do not each pay a full
       // gather latency in turn
       while (med) {
@@ -461,7 +548,8 @@ static int pr_launch(IgExec* ex, const ig_csr* dg, const int* d_degree, float* d
   const float base = (1.0f - damp) / (float)n;
   PrArgs a{dg->nindex, dg->nlist, d_degree, n, dg->edges, d_scores, (float*)ca, (float*)cb, (int*)hubs,
            (int*)cbase, (int*)chub, (float2*)part, (int*)blk, (double*)blkerr, ex->d_ctl, epsilon, max_iter, base, damp,
-           ex->timeout_ns, hub_degree, chunk, d_graph_vptr, graphs, (double*)gres, d_iters, (int*)vgraph};
+           ex->timeout_ns, hub_degree, chunk, o.pr_prefetch, o.pr_subwarp, d_graph_vptr, graphs, (double*)gres,
+           d_iters, (int*)vgraph};
   void* args[] = {&a};
   const int bps = o.pr_blocks_per_sm > 0 ? o.pr_blocks_per_sm : o.blocks_per_sm;
   const int cap = bps > 0 ? std::min(bps, 32) : 32;

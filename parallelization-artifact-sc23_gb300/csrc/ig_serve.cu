@@ -17,6 +17,15 @@
 // state cleared, and the lane admits the next pending query at the following
 // step boundary, while the other lanes keep going (continuous batching).
 // A worker thread owns the device work; clients submit and wait.
+//
+// Admission by device memory: an engine's state is allocated when a query of
+// its kind is pending and the device's free memory (less an eighth kept in
+// reserve) and the server's budget (ig_server_set_memory_budget) both cover
+// it.  Otherwise the query stays pending -- deferred, not failed -- and is
+// admitted when memory frees up: when the other engine falls idle it is
+// released to make room, and the worker retries each millisecond.  A query
+// whose engine can never fit the budget or the device fails with
+// IG_ERR_NOMEM.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -419,6 +428,7 @@ struct Request {
 
 struct Engine {
   int kind;                       // 0 BFS, 1 SSSP
+  bool live = false;              // state allocated
   Request* lane_req[kLanes] = {};
   u64 busy = 0;                   // lanes holding a query
   int step = 0;
@@ -453,11 +463,25 @@ struct ig_server {
   bool stop = false;
   int worker_rc = IG_OK;
   std::thread worker;
+  long long budget = -1;          // bytes the engines may hold together (-1: no cap)
+  long long deferrals = 0;        // admission attempts that found too little memory
+  long long engines_created = 0;
 };
+
+// Device bytes of one engine's state (engine_alloc's allocations).
+static long long engine_bytes(const ig_server* s, int kind) {
+  const long long n = s->g.nodes, vb = n * (long long)sizeof(int), mb = n * (long long)sizeof(u64);
+  long long b = 3 * vb + 64 + 2 * kLanes * sizeof(int) + 2 * mb;
+  if (kind == 0) b += 2 * mb + (long long)sizeof(BfsLaneState);
+  else b += n * kLanes * (long long)sizeof(int) + vb + vb + sizeof(int) + (long long)sizeof(SsspLaneState) +
+            kLanes * kMaxTargets * (long long)sizeof(int);
+  return b;
+}
 
 static int scuda(int e, const char* what) { return ig_cuda_check(e, what); }
 
 static int engine_alloc(ig_server* s, Engine& E, int kind) {
+  E.live = true;
   const int n = s->g.nodes;
   const size_t vb = (size_t)n * sizeof(int), mb = (size_t)n * sizeof(u64);
   E.kind = kind;
@@ -503,6 +527,78 @@ static void engine_free(Engine& E) {
                 E.deg, E.eoff, E.lane_state, E.tdist};
   for (void* p : ps)
     if (p) cudaFree(p);
+  const int kind = E.kind;
+  E = Engine();
+  E.kind = kind;
+}
+
+static void complete(ig_server* s, Request* r, const ig_query_result& res);
+
+// Makes engine k's state resident for its pending queries.  Returns IG_OK
+// when it is (or became) resident, IG_ERR_BUSY when the memory is short for
+// now (the queries stay pending), another status on a CUDA error.  Queries
+// whose engine can never fit fail with IG_ERR_NOMEM.
+static int engine_ensure(ig_server* s, int k) {
+  Engine& E = s->eng[k];
+  if (E.live) return IG_OK;
+  const long long need = engine_bytes(s, k);
+  size_t free_b = 0, total_b = 0;
+  int rc = scuda(cudaMemGetInfo(&free_b, &total_b), "cudaMemGetInfo");
+  if (rc) return rc;
+  long long budget;
+  {
+    std::lock_guard<std::mutex> lk(s->mu);
+    budget = s->budget;
+  }
+  const long long cap = budget >= 0 ? std::min<long long>(budget, (long long)total_b) : (long long)total_b;
+  if (need + (need >> 3) > cap) {  // never fits: fail this kind's pending queries
+    std::vector<Request*> drop;
+    {
+      std::lock_guard<std::mutex> lk(s->mu);
+      drop.assign(s->pending[k].begin(), s->pending[k].end());
+      s->pending[k].clear();
+    }
+    for (Request* r : drop) {
+      ig_query_result res;
+      memset(&res, 0, sizeof(res));
+      res.status = IG_ERR_NOMEM;
+      res.kind = r->kind;
+      res.source = r->source;
+      res.submit_time = r->submit_t;
+      res.done_time = now_s();
+      complete(s, r, res);
+    }
+    return IG_ERR_BUSY;
+  }
+  Engine& O = s->eng[1 - k];
+  auto fits = [&](long long free_now) {
+    const long long held = O.live ? engine_bytes(s, 1 - k) : 0;
+    return need + (need >> 3) <= free_now && (budget < 0 || held + need <= budget);
+  };
+  if (!fits((long long)free_b)) {
+    bool other_idle;
+    {
+      std::lock_guard<std::mutex> lk(s->mu);
+      other_idle = O.live && O.busy == 0 && s->pending[1 - k].empty();
+    }
+    if (other_idle) {  // release the idle engine to make room
+      if ((rc = scuda(cudaStreamSynchronize(s->stream), "sync"))) return rc;
+      engine_free(O);
+      if ((rc = scuda(cudaMemGetInfo(&free_b, &total_b), "cudaMemGetInfo"))) return rc;
+    }
+    if (!fits((long long)free_b)) {
+      std::lock_guard<std::mutex> lk(s->mu);
+      s->deferrals++;
+      return IG_ERR_BUSY;
+    }
+  }
+  if ((rc = engine_alloc(s, E, k))) {
+    engine_free(E);
+    return rc;
+  }
+  std::lock_guard<std::mutex> lk(s->mu);
+  s->engines_created++;
+  return IG_OK;
 }
 
 static void complete(ig_server* s, Request* r, const ig_query_result& res) {
@@ -776,10 +872,30 @@ static void worker_main(ig_server* s) {
       if (s->stop) break;
     }
     int rc = IG_OK;
+    bool progressed = false;
     for (int k = 0; k < 2 && rc == IG_OK; k++) {
       Engine& E = s->eng[k];
-      rc = engine_admit(s, E);
-      if (rc == IG_OK && E.busy) rc = (k == 0) ? bfs_step(s, E) : sssp_step(s, E);
+      bool want;
+      {
+        std::lock_guard<std::mutex> lk(s->mu);
+        want = !s->pending[k].empty();
+      }
+      if (want && !E.live) {
+        rc = engine_ensure(s, k);
+        if (rc == IG_ERR_BUSY) {  // deferred: too little memory for now
+          rc = IG_OK;
+          continue;
+        }
+      }
+      if (rc == IG_OK && E.live) rc = engine_admit(s, E);
+      if (rc == IG_OK && E.busy) {
+        rc = (k == 0) ? bfs_step(s, E) : sssp_step(s, E);
+        progressed = true;
+      }
+    }
+    if (rc == IG_OK && !progressed) {  // only deferred queries: wait for memory, then retry
+      std::unique_lock<std::mutex> lk(s->mu);
+      s->cv_work.wait_for(lk, std::chrono::milliseconds(1), [&] { return s->stop; });
     }
     std::lock_guard<std::mutex> lk(s->mu);
     s->steps++;
@@ -802,20 +918,20 @@ extern "C" int ig_server_create(const ig_csr* d_g, int max_pending, ig_server** 
   int rc;
   if ((rc = scuda(cudaGetDevice(&s->device), "cudaGetDevice"))) return rc;
   if ((rc = scuda(cudaDeviceGetAttribute(&s->sms, cudaDevAttrMultiProcessorCount, s->device), "SM count"))) return rc;
-  // Admission by device memory: both engines' state must fit with headroom.
+  // The engines' state is allocated when queries need it (engine_ensure);
+  // the smaller engine must at least fit the device now.
   size_t free_b = 0, total_b = 0;
   if ((rc = scuda(cudaMemGetInfo(&free_b, &total_b), "cudaMemGetInfo"))) return rc;
-  const size_t need = (size_t)d_g->nodes * (3 * sizeof(int) * 2 + 4 * sizeof(u64) + 2 * sizeof(u64) +
-                                            (d_g->eweight ? kLanes * sizeof(int) + sizeof(long long) + sizeof(int) : 0));
-  if (need + (need >> 3) > free_b)
-    return ig_fail(IG_ERR_NOMEM, "serving state needs %zu bytes, %zu free", need, free_b);
+  const long long need = engine_bytes(s.get(), 0);
+  if (need + (need >> 3) > (long long)free_b)
+    return ig_fail(IG_ERR_NOMEM, "serving state needs %lld bytes, %zu free", need, free_b);
+  s->eng[0].kind = 0;
+  s->eng[1].kind = 1;
   if ((rc = scuda(cudaStreamCreate(&s->stream), "stream"))) return rc;
   s->scratch.device = s->device;
   if ((rc = ig_exec_init(&s->ex, s->stream, &s->scratch, nullptr, s->device, s->sms))) return rc;
   s->d_ctl = s->ex.d_ctl;
   if ((rc = scuda(cudaMemsetAsync(s->d_ctl, 0, sizeof(IgCtl), s->stream), "memset"))) return rc;
-  if ((rc = engine_alloc(s.get(), s->eng[0], 0))) return rc;
-  if (d_g->eweight && (rc = engine_alloc(s.get(), s->eng[1], 1))) return rc;
   if ((rc = scuda(cudaStreamSynchronize(s->stream), "sync"))) return rc;
   ig_server* raw = s.release();
   raw->worker = std::thread(worker_main, raw);
@@ -869,6 +985,24 @@ extern "C" int ig_server_stats(ig_server* s, long long* completed, long long* st
   std::lock_guard<std::mutex> lk(s->mu);
   if (completed) *completed = s->completed;
   if (steps) *steps = s->steps;
+  return s->worker_rc;
+}
+
+extern "C" int ig_server_set_memory_budget(ig_server* s, long long bytes) {
+  if (!s || bytes < -1) return ig_fail(IG_ERR_INVALID_ARG, "ig_server_set_memory_budget: bad argument");
+  std::lock_guard<std::mutex> lk(s->mu);
+  s->budget = bytes;
+  s->cv_work.notify_all();
+  return IG_OK;
+}
+
+extern "C" int ig_server_memory(ig_server* s, long long* held_bytes, long long* deferrals, long long* engines_created) {
+  if (!s) return ig_fail(IG_ERR_INVALID_ARG, "null");
+  std::lock_guard<std::mutex> lk(s->mu);
+  if (held_bytes)
+    *held_bytes = (s->eng[0].live ? engine_bytes(s, 0) : 0) + (s->eng[1].live ? engine_bytes(s, 1) : 0);
+  if (deferrals) *deferrals = s->deferrals;
+  if (engines_created) *engines_created = s->engines_created;
   return s->worker_rc;
 }
 

@@ -164,6 +164,9 @@ SIGNATURES = {
     "ig_server_wait": (_I, [_P, ctypes.c_longlong, _I, ctypes.POINTER(QueryResult)]),
     "ig_server_stats": (_I, [_P, ctypes.POINTER(ctypes.c_longlong), ctypes.POINTER(ctypes.c_longlong)]),
     "ig_server_destroy": (_I, [_P]),
+    "ig_server_set_memory_budget": (_I, [_P, ctypes.c_longlong]),
+    "ig_server_memory": (_I, [_P, ctypes.POINTER(ctypes.c_longlong), ctypes.POINTER(ctypes.c_longlong),
+                              ctypes.POINTER(ctypes.c_longlong)]),
     "ig_gen_batch": (_I, [_I, _I, _I, ctypes.c_double, _I, ctypes.c_double, ctypes.c_double, ctypes.c_double, _U64,
                           _I, _PCSR, _P]),
 }

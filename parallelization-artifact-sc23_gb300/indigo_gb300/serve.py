@@ -78,6 +78,16 @@ class Server:
         check(load().ig_server_stats(self.h, ctypes.byref(c), ctypes.byref(s)))
         return c.value, s.value
 
+    def set_memory_budget(self, nbytes: int):
+        """Caps the device bytes the engines may hold together (-1: no cap)."""
+        check(load().ig_server_set_memory_budget(self.h, int(nbytes)))
+
+    def memory(self):
+        """(bytes the engines hold, admissions deferred for memory, engines created)."""
+        h, d, c = ctypes.c_longlong(), ctypes.c_longlong(), ctypes.c_longlong()
+        check(load().ig_server_memory(self.h, ctypes.byref(h), ctypes.byref(d), ctypes.byref(c)))
+        return h.value, d.value, c.value
+
     def close(self):
         if getattr(self, "h", None):
             load().ig_server_destroy(self.h)

@@ -364,3 +364,48 @@ def test_sssp_item_pass_forms(ig, orc, graphs, merge_below, spin):
     finally:
         for k, v in old.items():
             ig.set_option(k, v)
+
+
+@pytest.mark.parametrize("opt,values", [("bfs_bitmap", (0, 1)), ("cc_rounds", (0, 1))])
+def test_traversal_option_forms_match_oracle(ig, orc, graphs, opt, values):
+    """BFS with and without the level bitmaps of its bottom-up levels (forced
+    bottom-up from the first level too), CC with the sampled neighbours linked
+    in one pass or one round each: the results are exact every way."""
+    old = {k: ig.get_option(k) for k in (opt, "bfs_alpha")}
+    try:
+        for val in values:
+            ig.set_option(opt, val)
+            for alpha in (14, 1):
+                ig.set_option("bfs_alpha", alpha)
+                for name in ("rmat14", "hubby", "road128", "two_grids", "star"):
+                    g = graphs[name]
+                    r = run_all(ig, g, [0, g.nodes // 2])
+                    for k, s in enumerate([0, g.nodes // 2]):
+                        assert np.array_equal(r[f"bfs{k}"], orc.bfs(g, s)), (opt, val, alpha, name, s)
+                    assert np.array_equal(r["cc"], orc.cc(g)), (opt, val, name)
+    finally:
+        for k, v in old.items():
+            ig.set_option(k, v)
+
+
+@pytest.mark.parametrize("subwarp,prefetch", [(1, 1), (0, 0)])
+def test_pagerank_gather_forms(ig, orc, graphs, subwarp, prefetch):
+    """Medium lists summed by 8-lane sub-warps or by the whole warp, with or
+    without the L2 prefetch: within 1e-6 relative L1 of FP64, deterministic."""
+    old = (ig.get_option("pr_subwarp"), ig.get_option("pr_prefetch"))
+    try:
+        ig.set_option("pr_subwarp", subwarp)
+        ig.set_option("pr_prefetch", prefetch)
+        for name in ("rmat14", "hubby", "er4k", "rmat18"):
+            g = graphs[name]
+            outs = []
+            for _ in range(2):
+                s = np.full(g.nodes, np.float32(1.0) / np.float32(g.nodes), np.float32)
+                it, _ = ig.PR_GPU(g, s, g.degree(), 1e-6, 100)
+                outs.append(s)
+            assert np.array_equal(outs[0], outs[1]), name
+            ref, _, _ = orc.pr_f64(g, iters=it)
+            assert np.abs(outs[0] - ref).sum() / ref.sum() <= PR_TOL, name
+    finally:
+        ig.set_option("pr_subwarp", old[0])
+        ig.set_option("pr_prefetch", old[1])

@@ -90,3 +90,50 @@ def test_bad_queries_rejected(ig, served):
         srv.submit(2, 0)
     with pytest.raises(ig.IndigoError):
         srv.submit(0, 0, list(range(17)))
+
+
+def test_memory_admission_defers_then_serves(ig, orc, gpu):
+    """With a budget that holds only one engine, BFS and SSSP queries submitted
+    together cannot all be admitted at once: queries of the kind without an
+    engine are deferred (counted), not failed, until the resident engine
+    falls idle and is released; every answer still equals the oracle's."""
+    g = ig.rmat(13, 16, seed=19, maxw=1000)
+    with ig.DeviceCSR(g) as d:
+        srv = ig.Server(d, max_pending=256)
+        try:
+            srv.wait(srv.submit(1, 0))  # the SSSP engine, the larger one, is resident now
+            held_sssp, _, created0 = srv.memory()
+            assert held_sssp > 0 and created0 == 1
+            srv.set_memory_budget(held_sssp + 1024)  # room for one engine, not both
+            rng = np.random.default_rng(5)
+            srcs = [int(s) for s in g.pick_sources(24, seed=9)]
+            jobs = [(k, s, rng.integers(0, g.nodes, 3)) for s in srcs for k in (0, 1)]
+            tickets = [srv.submit(k, s, tg) for k, s, tg in jobs]
+            answers = [srv.wait(t, 120000) for t in tickets]
+            held, deferred, created = srv.memory()
+        finally:
+            srv.close()
+    assert deferred > 0 and created >= 2  # the SSSP engine released for the BFS engine
+    assert held <= held_sssp + 1024
+    for (k, s, tg), a in zip(jobs, answers):
+        dist = orc.bfs(g, s) if k == 0 else orc.sssp(g, s)
+        assert a.key() == ig.summarize(k, s, dist, tg).key(), (k, s)
+
+
+def test_memory_admission_fails_what_never_fits(ig, gpu):
+    """A budget below the SSSP engine's size: SSSP queries complete with
+    IG_ERR_NOMEM (they can never be admitted), BFS queries are served."""
+    g = ig.rmat(12, 16, seed=3, maxw=100)
+    with ig.DeviceCSR(g) as d:
+        srv = ig.Server(d, max_pending=64)
+        try:
+            srv.wait(srv.submit(0, 1))
+            held_bfs, _, _ = srv.memory()
+            srv.set_memory_budget(held_bfs + (held_bfs >> 2))
+            t_s = srv.submit(1, 1)
+            with pytest.raises(ig.IndigoError) as e:
+                srv.wait(t_s, 60000)
+            assert e.value.status == ig._lib.IG_ERR_NOMEM
+            assert srv.wait(srv.submit(0, 2), 60000).reached > 0
+        finally:
+            srv.close()
