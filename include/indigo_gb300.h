@@ -143,10 +143,12 @@ int ig_event_record(void* ev, void* stream);
 int ig_event_elapsed_ms(void* start, void* stop, float* ms);
 /* Bound (milliseconds) on every device-side wait; default 5000. */
 int ig_set_wait_timeout_ms(int ms);
-/* Kernel tuning knobs (process-wide): blocks_per_sm, bfs_alpha, bfs_beta,
- * hub_degree, sssp_delta, sssp_delta_scale, sssp_heavy_split,
- * sssp_item_edges, sssp_warp_degree, sssp_window_scale, sssp_window_degree,
- * pr_hub_degree, pr_chunk, pr_blocks_per_sm, tc_block_chunk. */
+/* Kernel tuning knobs (process-wide): blocks_per_sm, bfs_alpha (0: top-down
+ * only), bfs_beta, bfs_bitmap, hub_degree, sssp_delta, sssp_delta_scale,
+ * sssp_heavy_split, sssp_item_edges, sssp_warp_degree, sssp_window_scale,
+ * sssp_window_degree, sssp_merge_below, sssp_spin_ns, pr_hub_degree,
+ * pr_chunk, pr_blocks_per_sm, pr_prefetch, pr_subwarp, tc_block_chunk,
+ * cc_rounds.  Every setting gives the same results; they trade speed. */
 int ig_set_option(const char* name, long long value);
 int ig_get_option(const char* name, long long* value);
 /* Number of kernels this library has launched in the process. */
@@ -290,14 +292,21 @@ int ig_batch_tc(ig_batch* b, unsigned long long* d_counts);
 int ig_batch_pagerank(ig_batch* b, float* d_scores, float epsilon, int max_iter, int* d_iters);
 /* Autotuning of the batched form (no reference counterpart): for each
  * algorithm in algo_mask (bit 0 BFS, 1 CC, 2 TC, 3 PageRank) times a small set
- * of launch variants on this batch (blocks per SM, grid-expansion thresholds;
- * never a change of results), best of `reps` runs each, and keeps the fastest
- * for the batch's later calls.  best_ms[4] (may be NULL) receives the chosen
+ * of variants on this batch -- blocks per SM, grid-expansion thresholds
+ * (thread / warp / grid granularity), BFS push-pull against push-only levels
+ * and bitmap against distance tests in its pull levels, CC linking in one
+ * pass or in rounds, PageRank medium lists by warps or 8-lane sub-warps;
+ * never a change of results -- best of `reps` runs each, and keeps the
+ * fastest for the batch's later calls.  best_ms[4] (may be NULL) receives the chosen
  * variant's time per algorithm (-1 where not tuned).  Synchronous. */
 int ig_batch_autotune(ig_batch* b, int algo_mask, int reps, float* best_ms);
 /* The option value the batch uses for `algo` (0..3): the tuned one, else the
  * process-wide value (names as in ig_get_option). */
 int ig_batch_get_option(ig_batch* b, int algo, const char* name, long long* value);
+/* Sets one option for this batch's calls of algorithm `algo` (0 BFS, 1 CC,
+ * 2 TC, 3 PageRank; names as ig_set_option); a captured call is captured
+ * again.  Used to apply a stored tuning without timing. */
+int ig_batch_set_option(ig_batch* b, int algo, const char* name, long long value);
 /* Host generator of a batch: `graphs` graphs with vertex counts log-uniform
  * in [vmin, vmax]; even indices Erdos-Renyi (average degree er_degree), odd
  * ones RMAT (a, b, c; rmat_edge_factor pairs per vertex, ids taken modulo the

@@ -250,14 +250,34 @@ std::vector<IgOptions> batch_variants(int algo, const IgOptions& base) {
     out.push_back(o);
   };
   add(-1, 0, 0);  // the process-wide options first
+  // Besides residency and hub thresholds (thread / warp / grid granularity),
+  // the style axes: BFS push-pull (direction-optimising) against push only
+  // (data-driven worklist levels) and bitmap against distance tests in the
+  // bottom-up (pull, topology-driven) levels; CC sampled linking in one pass
+  // or one round per neighbour; PageRank medium lists by the warp or by
+  // 8-lane sub-warps.
   if (algo == kBfs) {
-    for (int bps : {2, 4, 8})
-      for (int hub : {128, 256, 1024}) add(bps, hub, 0);
+    for (int bps : {4, 8})
+      for (int hub : {256, 1024})
+        for (int alpha : {14, 0})
+          for (int bitmap : {1, 0}) {
+            add(bps, hub, 0);
+            out.back().bfs_alpha = alpha;
+            out.back().bfs_bitmap = bitmap;
+          }
   } else if (algo == kCc) {
-    for (int hub : {64, 256, 1024, 4096}) add(-1, hub, 0);
+    for (int hub : {64, 256, 1024, 4096})
+      for (int rounds : {0, 1}) {
+        add(-1, hub, 0);
+        out.back().cc_rounds = rounds;
+      }
   } else if (algo == kPr) {
-    for (int bps : {2, 3, 4, 8})
-      for (int ph : {1024, 4096}) add(bps, 0, ph);
+    for (int bps : {3, 4})
+      for (int ph : {1024, 4096})
+        for (int sub : {0, 1}) {
+          add(bps, 0, ph);
+          out.back().pr_subwarp = sub;
+        }
   }
   return out;  // TC: its launch shape follows the shared-memory tables; nothing to tune
 }
@@ -328,6 +348,20 @@ extern "C" int ig_batch_autotune(ig_batch* b, int algo_mask, int reps, float* be
   b->pending = false;
   b->last_rc = rc;
   return rc;
+}
+
+extern "C" int ig_batch_set_option(ig_batch* b, int algo, const char* name, long long value) {
+  if (!b || algo < 0 || algo >= kAlgos) return ig_fail(IG_ERR_INVALID_ARG, "ig_batch_set_option: bad argument");
+  IgOptions o = b->tuned[algo] ? b->opts[algo] : ig_options();
+  const int rc = ig_options_set(o, name, value);
+  if (rc) return rc;
+  b->opts[algo] = o;
+  b->tuned[algo] = true;
+  if (b->cap[algo].exec) {  // captured with the old options: capture again
+    cudaGraphExecDestroy(b->cap[algo].exec);
+    b->cap[algo].exec = nullptr;
+  }
+  return IG_OK;
 }
 
 extern "C" int ig_batch_get_option(ig_batch* b, int algo, const char* name, long long* value) {

@@ -189,7 +189,7 @@ __global__ void __launch_bounds__(kThreads) bfs_persistent(BfsArgs a) {
     unexplored -= mf;
     level = next_level;
     if (!bottom_up) {
-      if (mf > unexplored / a.alpha) bottom_up = true;
+      if (a.alpha > 0 && mf > unexplored / a.alpha) bottom_up = true;  // alpha 0: top-down only
     } else {
       if ((long long)nf * a.beta < a.nodes) bottom_up = false;
     }

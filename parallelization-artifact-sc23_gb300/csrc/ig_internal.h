@@ -103,6 +103,7 @@ struct IgExec {
 inline const IgOptions& ig_exec_options(const IgExec* ex) { return ex->opts ? *ex->opts : ig_options(); }
 // Reads option `name` of `o` (same names as ig_get_option).
 int ig_options_get(const IgOptions& o, const char* name, long long* value);
+int ig_options_set(IgOptions& o, const char* name, long long value);
 
 // Per-device state used by the drop-in entry points.
 struct IgDevice {

@@ -3,7 +3,7 @@
 
 struct IgOptions {
   int blocks_per_sm;      // cap on resident blocks per SM for persistent kernels (0 = occupancy)
-  int bfs_alpha;          // top-down -> bottom-up switch: frontier edges > unexplored / alpha
+  int bfs_alpha;          // top-down -> bottom-up switch: frontier edges > unexplored / alpha (0: never)
   int bfs_beta;           // bottom-up -> top-down switch: frontier vertices < V / beta
   int bfs_bitmap;         // 1: bottom-up levels test level bitmaps instead of neighbour distances
   int hub_degree;         // degree above which a vertex is expanded by the whole grid
@@ -23,6 +23,8 @@ struct IgOptions {
   int pr_blocks_per_sm;   // PageRank: resident blocks per SM (0 = blocks_per_sm)
   int pr_prefetch;        // PageRank: 1 = a warp prefetches its next lists into L2 while summing
   int pr_subwarp;         // PageRank: 1 = medium lists summed four at a time by 8-lane sub-warps
+  int pr_two_pass;        // PageRank: 1 = each iteration first gathers every edge's contribution in one
+                          // dense pass (128-bit loads and stores), then sums the lists from it
   int tc_block_chunk;     // TC: in-neighbours per block work item
   int cc_rounds;          // CC: 1 = sampled neighbours linked one round at a time (read-only root
                           // searches, a compression after each), 0 = both in one pass with path halving

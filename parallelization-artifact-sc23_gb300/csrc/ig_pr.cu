@@ -55,6 +55,7 @@ struct PrArgs {
   int chunk;
   int prefetch;  // 1: each warp prefetches its next vertex group's lists into L2
   int subwarp;   // 1: medium lists summed four at a time by 8-lane sub-warps (else two by the warp)
+  float* vals;   // two-pass form: vals[k] = contributions[nlist[k]], gathered each iteration (else null)
   // batched form (disjoint union of graphs): first vertex of each graph,
   // per-graph residuals (3 rotating slots) and per-graph iteration counts
   const int* graph_vptr;
@@ -104,10 +105,16 @@ __device__ __forceinline__ void warp_pair_reduce(float& hi, float& lo) {
   }
 }
 
-// Kahan sum of contrib[nlist[k]] over k = b + lane, b + lane + 32, ... < e,
-// returned as a (hi, lo) pair reduced over the warp (same value in all lanes).
-// Each lane keeps 8 gathers in flight and loads the next 8 indices while the
+// The value of edge slot k: contrib[nlist[k]], or, in the two-pass form,
+// vals[k], gathered for every edge by the iteration's first pass.  The
+// kTwo forms below read vals (written in this kernel: plain loads) and
+// skip the index loads; the order of the adds is the same either way.
+//
+// Kahan sum of the values of k = b + lane, b + lane + 32, ... < e, returned
+// as a (hi, lo) pair reduced over the warp (same value in all lanes).  Each
+// lane keeps 8 gathers in flight and loads the next 8 indices while the
 // current values arrive; the adds stay in the order k, k + 32, k + 64, ...
+template <bool kTwo>
 __device__ __forceinline__ void warp_gather_sum(const int* __restrict__ nlist, const float* contrib, int b, int e,
                                                 float& hi, float& lo) {
   constexpr int kDepth = 8;
@@ -115,14 +122,14 @@ __device__ __forceinline__ void warp_gather_sum(const int* __restrict__ nlist, c
   int k = b + ig::lane_id();
   int n[kDepth];
 #pragma unroll
-  for (int t = 0; t < kDepth; t++) n[t] = k + 32 * t < e ? __ldg(&nlist[k + 32 * t]) : 0;
+  for (int t = 0; t < kDepth; t++) n[t] = (!kTwo && k + 32 * t < e) ? __ldg(&nlist[k + 32 * t]) : 0;
   while (k < e) {
     float x[kDepth];
 #pragma unroll
-    for (int t = 0; t < kDepth; t++) x[t] = k + 32 * t < e ? contrib[n[t]] : 0.f;
+    for (int t = 0; t < kDepth; t++) x[t] = k + 32 * t < e ? contrib[kTwo ? k + 32 * t : n[t]] : 0.f;
     const int kn = k + 32 * kDepth;
 #pragma unroll
-    for (int t = 0; t < kDepth; t++) n[t] = kn + 32 * t < e ? __ldg(&nlist[kn + 32 * t]) : 0;
+    for (int t = 0; t < kDepth; t++) n[t] = (!kTwo && kn + 32 * t < e) ? __ldg(&nlist[kn + 32 * t]) : 0;
 #pragma unroll
     for (int t = 0; t < kDepth; t++)
       if (k + 32 * t < e) kahan_add(s, c, x[t]);
@@ -137,6 +144,7 @@ __device__ __forceinline__ void warp_gather_sum(const int* __restrict__ nlist, c
 // gathers are issued together (4 in flight per lane for each), each with its
 // own Kahan sum in the same per-lane order as warp_gather_sum, so the results
 // are the same bits.
+template <bool kTwo>
 __device__ __forceinline__ void warp_gather_sum2(const int* __restrict__ nlist, const float* contrib, int b1, int e1,
                                                  int b2, int e2, float& hi1, float& lo1, float& hi2, float& lo2) {
   constexpr int kDepth = 4;
@@ -146,14 +154,14 @@ __device__ __forceinline__ void warp_gather_sum2(const int* __restrict__ nlist, 
     int n1[kDepth], n2[kDepth];
 #pragma unroll
     for (int t = 0; t < kDepth; t++) {
-      n1[t] = k1 + 32 * t < e1 ? __ldg(&nlist[k1 + 32 * t]) : 0;
-      n2[t] = k2 + 32 * t < e2 ? __ldg(&nlist[k2 + 32 * t]) : 0;
+      n1[t] = (!kTwo && k1 + 32 * t < e1) ? __ldg(&nlist[k1 + 32 * t]) : 0;
+      n2[t] = (!kTwo && k2 + 32 * t < e2) ? __ldg(&nlist[k2 + 32 * t]) : 0;
     }
     float x1[kDepth], x2[kDepth];
 #pragma unroll
     for (int t = 0; t < kDepth; t++) {
-      x1[t] = k1 + 32 * t < e1 ? contrib[n1[t]] : 0.f;
-      x2[t] = k2 + 32 * t < e2 ? contrib[n2[t]] : 0.f;
+      x1[t] = k1 + 32 * t < e1 ? contrib[kTwo ? k1 + 32 * t : n1[t]] : 0.f;
+      x2[t] = k2 + 32 * t < e2 ? contrib[kTwo ? k2 + 32 * t : n2[t]] : 0.f;
     }
 #pragma unroll
     for (int t = 0; t < kDepth; t++) {
@@ -171,12 +179,15 @@ __device__ __forceinline__ void warp_gather_sum2(const int* __restrict__ nlist, 
   warp_pair_reduce(hi2, lo2);
 }
 
-// Asks L2 to fetch nlist[b, e) ahead of its use (cp.async.bulk.prefetch, 16-byte
-// granules inside the array; no register holds the data, nothing waits on it).
-__device__ __forceinline__ void prefetch_list(const PrArgs& a, int b, int e) {
-  const unsigned long long lo = (unsigned long long)(a.nlist + b) & ~15ull;
-  const unsigned long long end = (unsigned long long)(a.nlist + a.edges) & ~15ull;
-  unsigned long long hi = ((unsigned long long)(a.nlist + e) + 15ull) & ~15ull;
+// Asks L2 to fetch list[b, e) of a per-edge array (nlist, or the gathered
+// values of the two-pass form) ahead of its use (cp.async.bulk.prefetch,
+// 16-byte granules inside the array; no register holds the data, nothing
+// waits on it).
+__device__ __forceinline__ void prefetch_list(const PrArgs& a, const void* list, int b, int e) {
+  const int* p = (const int*)list;
+  const unsigned long long lo = (unsigned long long)(p + b) & ~15ull;
+  const unsigned long long end = (unsigned long long)(p + a.edges) & ~15ull;
+  unsigned long long hi = ((unsigned long long)(p + e) + 15ull) & ~15ull;
   if (hi > end) hi = end;
   if (e > b && hi > lo)
     asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(lo), "r"((unsigned)(hi - lo)) : "memory");
@@ -188,6 +199,7 @@ __device__ __forceinline__ void prefetch_list(const PrArgs& a, int b, int e) {
 // in flight and loads the next 8 indices while the current values arrive.
 // The order depends only on [b, e), so a vertex's sum is the same wherever
 // its list lies.
+template <bool kTwo>
 __device__ __forceinline__ void subwarp8_gather_sum(const int* __restrict__ nlist, const float* contrib, int b, int e,
                                                     float& hi, float& lo) {
   constexpr int kDepth = 8, kW = 8;
@@ -195,14 +207,14 @@ __device__ __forceinline__ void subwarp8_gather_sum(const int* __restrict__ nlis
   int k = b + (ig::lane_id() & (kW - 1));
   int n[kDepth];
 #pragma unroll
-  for (int t = 0; t < kDepth; t++) n[t] = k + kW * t < e ? __ldg(&nlist[k + kW * t]) : 0;
+  for (int t = 0; t < kDepth; t++) n[t] = (!kTwo && k + kW * t < e) ? __ldg(&nlist[k + kW * t]) : 0;
   while (k < e) {  // lanes of a sub-warp may leave at different steps: no collectives inside
     float x[kDepth];
 #pragma unroll
-    for (int t = 0; t < kDepth; t++) x[t] = k + kW * t < e ? contrib[n[t]] : 0.f;
+    for (int t = 0; t < kDepth; t++) x[t] = k + kW * t < e ? contrib[kTwo ? k + kW * t : n[t]] : 0.f;
     const int kn = k + kW * kDepth;
 #pragma unroll
-    for (int t = 0; t < kDepth; t++) n[t] = kn + kW * t < e ? __ldg(&nlist[kn + kW * t]) : 0;
+    for (int t = 0; t < kDepth; t++) n[t] = (!kTwo && kn + kW * t < e) ? __ldg(&nlist[kn + kW * t]) : 0;
 #pragma unroll
     for (int t = 0; t < kDepth; t++)
       if (k + kW * t < e) kahan_add(s, c, x[t]);
@@ -222,8 +234,8 @@ __device__ __forceinline__ int vdegree(const PrArgs& a, int v) {
   return a.degree ? a.degree[v] : (__ldg(&a.nindex[v + 1]) - __ldg(&a.nindex[v]));
 }
 
-template <bool kBatched>
-__global__ void __launch_bounds__(kThreads) pr_persistent(PrArgs a) {
+template <bool kBatched, bool kTwo>
+__global__ void __launch_bounds__(kThreads, 4) pr_persistent(PrArgs a) {
   using namespace ig;
   __shared__ int s_scan[33];
   __shared__ double s_red[32];
@@ -319,6 +331,33 @@ __global__ void __launch_bounds__(kThreads) pr_persistent(PrArgs a) {
       for (long long g = gtid; g < a.graphs; g += gthreads) gnext[g] = 0.0;
     }
     auto frozen = [&](int g) { return kBatched && it > 1 && ld_relaxed(&gprev[g]) < (double)a.eps; };
+    if (kTwo) {
+      // ---- first pass: the contribution of every edge slot, vals[k] =
+      // cur[nlist[k]], through 128-bit index loads and 128-bit stores (both
+      // arrays 16-byte aligned, checked at launch), four quads per thread in
+      // flight: the gathers of the iteration issued as one dense stream
+      const long long nq = a.edges >> 2;
+      const int4* nl4 = reinterpret_cast<const int4*>(a.nlist);
+      float4* v4 = reinterpret_cast<float4*>(a.vals);
+      for (long long q0 = gtid; q0 < nq; q0 += 4 * gthreads) {
+        int4 ix[4];
+#pragma unroll
+        for (int u = 0; u < 4; u++) {
+          const long long q = q0 + u * gthreads;
+          ix[u] = q < nq ? __ldg(&nl4[q]) : make_int4(0, 0, 0, 0);
+        }
+        float4 x[4];
+#pragma unroll
+        for (int u = 0; u < 4; u++) x[u] = make_float4(cur[ix[u].x], cur[ix[u].y], cur[ix[u].z], cur[ix[u].w]);
+#pragma unroll
+        for (int u = 0; u < 4; u++) {
+          const long long q = q0 + u * gthreads;
+          if (q < nq) v4[q] = x[u];
+        }
+      }
+      for (long long k = (nq << 2) + gtid; k < a.edges; k += gthreads) a.vals[k] = cur[__ldg(&a.nlist[k])];
+      if (!grid_sync(ctl, a.timeout_ns)) return;
+    }
     // ---- phase A: hub chunks (partial sums) and regular vertices
     for (int c = warp_g; c < nchunks; c += nwarps) {
       const int lo = a.chunk_hub[c];  // owning hub
@@ -328,7 +367,7 @@ __global__ void __launch_bounds__(kThreads) pr_persistent(PrArgs a) {
       const int b = hb + (c - a.chunk_base[lo]) * a.chunk;
       const int e = min(b + a.chunk, he);
       float shi, slo;
-      warp_gather_sum(a.nlist, cur, b, e, shi, slo);
+      warp_gather_sum<kTwo>(a.nlist, kTwo ? a.vals : cur, b, e, shi, slo);
       if (lane == 0) a.partial[c] = make_float2(shi, slo);
     }
     // each lane's list range of the warp's next group is loaded (and its list
@@ -339,7 +378,7 @@ __global__ void __launch_bounds__(kThreads) pr_persistent(PrArgs a) {
       if (v0 < a.nodes) {
         nb = __ldg(&a.nindex[v0]);
         ne = __ldg(&a.nindex[v0 + 1]);
-        if (a.prefetch && ne - nb <= a.hub_degree) prefetch_list(a, nb, ne);
+        if (a.prefetch && ne - nb <= a.hub_degree) prefetch_list(a, kTwo ? (const void*)a.vals : a.nlist, nb, ne);
       }
     }
     for (long long base = (long long)warp_g * 32; base < a.nodes; base += (long long)nwarps * 32) {
@@ -352,7 +391,7 @@ __global__ void __launch_bounds__(kThreads) pr_persistent(PrArgs a) {
         if (vn < a.nodes) {
           nb = __ldg(&a.nindex[vn]);
           ne = __ldg(&a.nindex[vn + 1]);
-          if (a.prefetch && ne - nb <= a.hub_degree) prefetch_list(a, nb, ne);
+          if (a.prefetch && ne - nb <= a.hub_degree) prefetch_list(a, kTwo ? (const void*)a.vals : a.nlist, nb, ne);
         }
       }
       int d = e - b;
@@ -376,10 +415,10 @@ __global__ void __launch_bounds__(kThreads) pr_persistent(PrArgs a) {
         for (int k = b; k < e; k += 8) {
           int nb[8];
 #pragma unroll
-          for (int t = 0; t < 8; t++) nb[t] = k + t < e ? __ldg(&a.nlist[k + t]) : -1;
+          for (int t = 0; t < 8; t++) nb[t] = k + t < e ? (kTwo ? k + t : __ldg(&a.nlist[k + t])) : -1;
           float x[8];
 #pragma unroll
-          for (int t = 0; t < 8; t++) x[t] = nb[t] >= 0 ? cur[nb[t]] : 0.f;
+          for (int t = 0; t < 8; t++) x[t] = nb[t] >= 0 ? (kTwo ? a.vals : cur)[nb[t]] : 0.f;
 #pragma unroll
           for (int t = 0; t < 8; t++)
             if (nb[t] >= 0) kahan_add(s, c, x[t]);
@@ -400,7 +439,7 @@ __global__ void __launch_bounds__(kThreads) pr_persistent(PrArgs a) {
         const int mb = __shfl_sync(IG_FULL, b, mine < 0 ? 0 : mine);
         const int me = __shfl_sync(IG_FULL, e, mine < 0 ? 0 : mine);
         float h, l;
-        subwarp8_gather_sum(a.nlist, cur, mb, mine < 0 ? mb : me, h, l);
+        subwarp8_gather_sum<kTwo>(a.nlist, kTwo ? a.vals : cur, mb, mine < 0 ? mb : me, h, l);
         const float tot = __fadd_rn(h, l);
 #pragma unroll
         for (int r = 0; r < 4; r++) {
@@ -419,7 +458,7 @@ __global__ void __launch_bounds__(kThreads) pr_persistent(PrArgs a) {
         int mb2 = __shfl_sync(IG_FULL, b, l2), me2 = __shfl_sync(IG_FULL, e, l2);
         if (l2 == l1) me2 = mb2;  // no second vertex
         float h1, o1, h2, o2;
-        warp_gather_sum2(a.nlist, cur, mb1, me1, mb2, me2, h1, o1, h2, o2);
+        warp_gather_sum2<kTwo>(a.nlist, kTwo ? a.vals : cur, mb1, me1, mb2, me2, h1, o1, h2, o2);
         if (lane == l1) sum = __fadd_rn(h1, o1);
         if (l2 != l1 && lane == l2) sum = __fadd_rn(h2, o2);
       }
@@ -535,6 +574,10 @@ static int pr_launch(IgExec* ex, const ig_csr* dg, const int* d_degree, float* d
   if ((rc = ig_scratch_get(ex->scratch, IG_SLOT_Q3, (size_t)max_chunks * sizeof(int), &chub))) return rc;
   if ((rc = ig_scratch_get(ex->scratch, IG_SLOT_V0, (size_t)2 * max_blocks * sizeof(int), &blk))) return rc;
   if ((rc = ig_scratch_get(ex->scratch, IG_SLOT_BLK, (size_t)2 * max_blocks * sizeof(double), &blkerr))) return rc;
+  // two-pass form: edge values gathered in one dense pass (needs a 16-byte aligned nlist)
+  void* vals = nullptr;
+  const bool two = o.pr_two_pass && dg->edges > 0 && ((uintptr_t)dg->nlist & 15) == 0;
+  if (two && (rc = ig_scratch_get(ex->scratch, IG_SLOT_E0, (size_t)dg->edges * sizeof(float), &vals))) return rc;
   if (d_graph_vptr) {
     if ((rc = ig_scratch_get(ex->scratch, IG_SLOT_V1, (size_t)3 * graphs * sizeof(double), &gres))) return rc;
     if ((rc = ig_scratch_get(ex->scratch, IG_SLOT_G2, (size_t)n * sizeof(int), &vgraph))) return rc;
@@ -548,12 +591,13 @@ static int pr_launch(IgExec* ex, const ig_csr* dg, const int* d_degree, float* d
   const float base = (1.0f - damp) / (float)n;
   PrArgs a{dg->nindex, dg->nlist, d_degree, n, dg->edges, d_scores, (float*)ca, (float*)cb, (int*)hubs,
            (int*)cbase, (int*)chub, (float2*)part, (int*)blk, (double*)blkerr, ex->d_ctl, epsilon, max_iter, base, damp,
-           ex->timeout_ns, hub_degree, chunk, o.pr_prefetch, o.pr_subwarp, d_graph_vptr, graphs, (double*)gres,
-           d_iters, (int*)vgraph};
+           ex->timeout_ns, hub_degree, chunk, o.pr_prefetch, o.pr_subwarp, (float*)vals, d_graph_vptr, graphs,
+           (double*)gres, d_iters, (int*)vgraph};
   void* args[] = {&a};
   const int bps = o.pr_blocks_per_sm > 0 ? o.pr_blocks_per_sm : o.blocks_per_sm;
   const int cap = bps > 0 ? std::min(bps, 32) : 32;
-  const void* fn = d_graph_vptr ? (const void*)pr_persistent<true> : (const void*)pr_persistent<false>;
+  const void* fn = d_graph_vptr ? (two ? (const void*)pr_persistent<true, true> : (const void*)pr_persistent<true, false>)
+                                : (two ? (const void*)pr_persistent<false, true> : (const void*)pr_persistent<false, false>);
   return ig_launch_coop(ex, fn, kThreads, 0, cap, args, nullptr);
 }
 

@@ -668,7 +668,8 @@ IgOptions& ig_options() {
       /*pr_chunk=*/4096,
       /*pr_blocks_per_sm=*/4,
       /*pr_prefetch=*/1,
-      /*pr_subwarp=*/0,
+      /*pr_subwarp=*/1,
+      /*pr_two_pass=*/1,
       /*tc_block_chunk=*/4096,
       /*cc_rounds=*/0,
   };
@@ -685,27 +686,29 @@ struct OptField {
   {#field, lo, hi, [](IgOptions& o, long long v) { o.field = (decltype(o.field))v; }, \
    [](const IgOptions& o) { return (long long)o.field; }}
 static const OptField g_opt_fields[] = {
-    IG_OPT(blocks_per_sm, 0, 32),     IG_OPT(bfs_alpha, 1, 1000000),   IG_OPT(bfs_beta, 1, 1000000), IG_OPT(bfs_bitmap, 0, 1),
+    IG_OPT(blocks_per_sm, 0, 32),     IG_OPT(bfs_alpha, 0, 1000000),   IG_OPT(bfs_beta, 1, 1000000), IG_OPT(bfs_bitmap, 0, 1),
     IG_OPT(hub_degree, 32, INT_MAX),  IG_OPT(sssp_delta, 0, INT_MAX),  IG_OPT(sssp_delta_scale, 1, 1 << 20),
     IG_OPT(sssp_heavy_split, 0, 1),   IG_OPT(sssp_item_edges, 32, 4096), IG_OPT(sssp_warp_degree, 1, INT_MAX),
     IG_OPT(sssp_window_scale, 0, 1 << 20), IG_OPT(sssp_window_degree, 0, INT_MAX),
     IG_OPT(sssp_merge_below, 0, INT_MAX),   IG_OPT(sssp_spin_ns, 0, 100000),
     IG_OPT(pr_hub_degree, 32, INT_MAX), IG_OPT(pr_chunk, 32, 1 << 24),
-    IG_OPT(pr_blocks_per_sm, 0, 32), IG_OPT(pr_prefetch, 0, 1), IG_OPT(pr_subwarp, 0, 1), IG_OPT(tc_block_chunk, 256, 1 << 16), IG_OPT(cc_rounds, 0, 1),
+    IG_OPT(pr_blocks_per_sm, 0, 32), IG_OPT(pr_prefetch, 0, 1), IG_OPT(pr_subwarp, 0, 1), IG_OPT(pr_two_pass, 0, 1), IG_OPT(tc_block_chunk, 256, 1 << 16), IG_OPT(cc_rounds, 0, 1),
 };
 
-extern "C" int ig_set_option(const char* name, long long value) {
+int ig_options_set(IgOptions& o, const char* name, long long value) {
   if (!name) return ig_fail(IG_ERR_INVALID_ARG, "null option name");
   for (const auto& f : g_opt_fields) {
     if (strcmp(f.name, name) == 0) {
       if (value < f.lo || value > f.hi)
         return ig_fail(IG_ERR_INVALID_ARG, "option %s out of range [%lld, %lld]", name, f.lo, f.hi);
-      f.set(ig_options(), value);
+      f.set(o, value);
       return IG_OK;
     }
   }
   return ig_fail(IG_ERR_INVALID_ARG, "unknown option %s", name);
 }
+
+extern "C" int ig_set_option(const char* name, long long value) { return ig_options_set(ig_options(), name, value); }
 
 int ig_options_get(const IgOptions& o, const char* name, long long* value) {
   if (!name || !value) return ig_fail(IG_ERR_INVALID_ARG, "null argument");

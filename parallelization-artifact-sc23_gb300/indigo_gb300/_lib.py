@@ -159,6 +159,7 @@ SIGNATURES = {
     "ig_batch_pagerank": (_I, [_P, _P, ctypes.c_float, _I, _P]),
     "ig_batch_autotune": (_I, [_P, _I, _I, _P]),
     "ig_batch_get_option": (_I, [_P, _I, ctypes.c_char_p, _P]),
+    "ig_batch_set_option": (_I, [_P, _I, ctypes.c_char_p, ctypes.c_longlong]),
     "ig_server_create": (_I, [_PCSR, _I, ctypes.POINTER(_P)]),
     "ig_server_submit": (_I, [_P, _I, _I, _P, _I, ctypes.POINTER(ctypes.c_longlong)]),
     "ig_server_wait": (_I, [_P, ctypes.c_longlong, _I, ctypes.POINTER(QueryResult)]),

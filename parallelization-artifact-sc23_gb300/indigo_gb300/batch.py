@@ -5,6 +5,9 @@ first call."""
 from __future__ import annotations
 
 import ctypes
+import json
+import math
+import os
 
 import numpy as np
 
@@ -115,16 +118,61 @@ class Batch:
         check(load().ig_batch_pagerank(self.h, scores.ptr, epsilon, max_iter, iters.ptr))
 
     ALGOS = ("bfs", "cc", "tc", "pr")
+    # the options the autotuner chooses, per algorithm (the style axes and knobs it varies)
+    TUNED = {"bfs": ("blocks_per_sm", "hub_degree", "bfs_alpha", "bfs_bitmap"),
+             "cc": ("hub_degree", "cc_rounds"),
+             "tc": (),
+             "pr": ("pr_blocks_per_sm", "pr_hub_degree", "pr_subwarp")}
 
-    def autotune(self, algos=("bfs", "cc", "pr"), reps: int = 2) -> dict:
-        """Times the launch variants of each algorithm on this batch and keeps
-        the fastest for later calls; returns {algo: best ms}."""
-        mask = 0
+    def stats_key(self) -> str:
+        """The tuning database's key for this batch: log2 buckets of the graph
+        count, the mean vertex count and the mean degree."""
+        v = self.nodes / max(1, self.graphs)
+        deg = self.union.edges / max(1, self.nodes)
+        return "g%d_v%d_d%d" % (round(math.log2(max(1, self.graphs))), round(math.log2(max(1.0, v))),
+                                round(math.log2(max(1.0, deg))))
+
+    def autotune(self, algos=("bfs", "cc", "pr"), reps: int = 2, db: str | None = None) -> dict:
+        """Times the variants of each algorithm on this batch and keeps the
+        fastest for later calls; returns {algo: best ms}.  With `db` (a JSON
+        file path), a batch whose statistics key is stored there takes the
+        stored options without timing (then ms is None), and a newly tuned
+        choice is stored under its key."""
+        table = {}
+        if db and os.path.exists(db):
+            with open(db) as f:
+                table = json.load(f)
+        key = self.stats_key()
+        stored = table.get(key, {})
+        out = {}
+        todo = []
         for a in algos:
-            mask |= 1 << self.ALGOS.index(a)
-        best = (ctypes.c_float * 4)()
-        check(load().ig_batch_autotune(self.h, mask, reps, best))
-        return {a: float(best[i]) for i, a in enumerate(self.ALGOS) if mask & (1 << i)}
+            if a in stored:
+                for name, value in stored[a].items():
+                    self.set_option(a, name, int(value))
+                out[a] = None
+            else:
+                todo.append(a)
+        if todo:
+            mask = 0
+            for a in todo:
+                mask |= 1 << self.ALGOS.index(a)
+            best = (ctypes.c_float * 4)()
+            check(load().ig_batch_autotune(self.h, mask, reps, best))
+            for a in todo:
+                out[a] = float(best[self.ALGOS.index(a)])
+            if db:
+                entry = table.setdefault(key, {})
+                for a in todo:
+                    entry[a] = {n: self.get_option(a, n) for n in self.TUNED[a]}
+                tmp = db + ".tmp"
+                with open(tmp, "w") as f:
+                    json.dump(table, f, indent=1, sort_keys=True)
+                os.replace(tmp, db)
+        return out
+
+    def set_option(self, algo: str, name: str, value: int):
+        check(load().ig_batch_set_option(self.h, self.ALGOS.index(algo), name.encode(), int(value)))
 
     def get_option(self, algo: str, name: str) -> int:
         v = ctypes.c_longlong()

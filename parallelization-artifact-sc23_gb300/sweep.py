@@ -1,19 +1,21 @@
-"""Variant sweep: every algorithm under each of its kernel-option variants
-(the GB300 counterparts of the suite's style axes), timed on one graph and
-written in the layout of the reference's result tables (data/<algo>_cuda.csv:
-a "filename" column naming graph, GPU and variant, and a column holding the
-throughput in gigaedges per second that the drivers print, E / runtime).
+"""Variant sweep over the suite's style axes: every algorithm under each
+combination of its axes -- the GB300 counterparts of the paper's vertex /
+edge parallel, push / pull, data- / topology-driven and thread / warp /
+block granularity choices -- timed on one graph and written in the layout of
+the reference's result tables (data/<algo>_cuda.csv: a "filename" column
+naming graph, GPU and variant, and a column holding the throughput in
+gigaedges per second that the drivers print, E / runtime).
 
     python parallelization-artifact-sc23_gb300/sweep.py --graph rmat:20 --algos bfs,sssp \
         --out sweep.csv [--repeat 5] [--compare data/bfs_cuda.csv]
 
 Variants differ only in speed: the sweep checks that every variant returns
 the same result (bit for bit; PageRank within 1e-6 relative L1 of the first
-variant) before it reports a number.  --compare prints, beside each
-algorithm's best variant, the best row of a reference table for the same
-algorithm (the caller names the file; the reference's graphs are not
-generated here, so the comparison is across graphs unless the caller loads
-the same .egr)."""
+variant) before it reports a number (the GPU tests check every variant
+against the oracle instead).  --compare prints, beside each algorithm's best
+variant, the best row of a reference table for the same algorithm (the
+caller names the file; the reference's graphs are not generated here, so the
+comparison is across graphs unless the caller loads the same .egr)."""
 from __future__ import annotations
 
 import argparse
@@ -28,34 +30,74 @@ sys.path.insert(0, str(Path(__file__).resolve().parent))
 
 import indigo_gb300 as ig  # noqa: E402
 
-# Option grids per algorithm.  The first entry of every grid is the library
-# default, so the first variant is the default configuration.
-AXES = {
-    "bfs": {"blocks_per_sm": [4, 2, 8], "hub_degree": [256, 64, 1024], "bfs_alpha": [14, 1000000]},
-    "sssp": {"blocks_per_sm": [4, 3], "sssp_item_edges": [256, 512], "sssp_window_scale": [8, 4, 0],
-             "sssp_window_degree": [16, 64], "sssp_delta_scale": [128, 32], "sssp_heavy_split": [0, 1]},
-    "cc": {"blocks_per_sm": [4, 8], "hub_degree": [256, 64, 4096]},
-    "mis": {"blocks_per_sm": [4, 2, 8]},
-    "pr": {"pr_blocks_per_sm": [4, 3, 2], "pr_hub_degree": [1024, 256, 4096], "pr_chunk": [4096, 512]},
-    "tc": {"tc_block_chunk": [4096, 1024]},
+BIG = 1 << 30
+# Style axes per algorithm: axis -> {style word: kernel options}.  The first
+# word of every axis is the library default, so the first variant is the
+# default configuration.  Words follow the suite's file names (V / E, Push /
+# Pull, Data / Topo, Thread / Warp / Block) where the GB300 design has the
+# counterpart:
+#   BFS  direction: PushPull = direction-optimising (data-driven top-down
+#        worklist levels, topology-driven bottom-up levels), Push = top-down
+#        only (Data), Pull = bottom-up as soon as the frontier has edges,
+#        back to top-down only for the small last levels (Topo);
+#        granularity: lists expanded by the warp's lanes, with lists above the
+#        hub degree spread over the whole grid (WarpGrid), warp only, or
+#        grid-wide for every list above 32 (Grid); Bitmap / Dist: how a pull
+#        level tests a neighbour.
+#   SSSP parallel: V = each vertex's list expanded by the warp that holds it,
+#        E = every list cut into edge work items, VE = lists above 64 edges as
+#        work items (default); order: Window = long lists expanded near
+#        Dijkstra order, NoWindow; sync: Sync2 = work items after a second
+#        grid barrier per round, Sync1 = within the round (one barrier);
+#        Plain / LightHeavy edge split.  (Always a data-driven worklist.)
+#   CC   link: Pass = sampled neighbours linked in one pass with path
+#        halving, Rounds = one round per neighbour with a compression after
+#        each; granularity as BFS.  (Hooking pushes along edges.)
+#   MIS  residency only (B4 / B2 / B8 blocks per SM).
+#   PR   gather: TwoPass = every edge's contribution gathered first in one
+#        dense pass, OnePass = gathered while summing; granularity: SubWarp =
+#        medium lists four at a time by 8-lane sub-warps, WarpPair = by the
+#        whole warp two at a time; hub chunks of 1024 /
+#        4096 / 256 edges; Prefetch / NoPrefetch of each warp's next lists.
+#        (Pull only: push PageRank needs float atomics, not deterministic.)
+#   TC   block work items of 4096 / 1024 in-neighbours.
+STYLES = {
+    "bfs": {"direction": {"PushPull": {}, "Push": {"bfs_alpha": 0}, "Pull": {"bfs_alpha": 1000000}},
+            "granularity": {"WarpGrid": {}, "Warp": {"hub_degree": BIG}, "Grid": {"hub_degree": 32}},
+            "test": {"Bitmap": {}, "Dist": {"bfs_bitmap": 0}}},
+    "sssp": {"parallel": {"VE": {}, "V": {"sssp_warp_degree": BIG}, "E": {"sssp_warp_degree": 1}},
+             "order": {"Window": {}, "NoWindow": {"sssp_window_scale": 0}},
+             "sync": {"Sync2": {}, "Sync1": {"sssp_merge_below": BIG}},
+             "split": {"Plain": {}, "LightHeavy": {"sssp_heavy_split": 1}}},
+    "cc": {"link": {"Pass": {}, "Rounds": {"cc_rounds": 1}},
+           "granularity": {"WarpGrid": {}, "Grid": {"hub_degree": 64}, "Warp": {"hub_degree": BIG}}},
+    "mis": {"residency": {"B4": {}, "B2": {"blocks_per_sm": 2}, "B8": {"blocks_per_sm": 8}}},
+    "pr": {"gather": {"TwoPass": {}, "OnePass": {"pr_two_pass": 0}},
+           "granularity": {"SubWarp": {}, "WarpPair": {"pr_subwarp": 0}},
+           "hubs": {"Chunk1024": {}, "Chunk4096": {"pr_hub_degree": 4096}, "Chunk256": {"pr_hub_degree": 256}},
+           "prefetch": {"Prefetch": {}, "NoPrefetch": {"pr_prefetch": 0}}},
+    "tc": {"items": {"Item4096": {}, "Item1024": {"tc_block_chunk": 1024}}},
 }
-# short labels for the variant names (like the suite's style words)
-LABEL = {"blocks_per_sm": "B", "hub_degree": "Hub", "bfs_alpha": "Alpha", "sssp_item_edges": "Item",
-         "sssp_warp_degree": "Warp", "sssp_window_scale": "Win", "sssp_window_degree": "WinDeg",
-         "sssp_delta_scale": "Delta", "sssp_heavy_split": "Split", "pr_blocks_per_sm": "B",
-         "pr_hub_degree": "Hub", "pr_chunk": "Chunk", "tc_block_chunk": "Item"}
+AXES = STYLES  # the per-algorithm axes (name kept for callers)
+OPTION_NAMES = sorted({k for axes in STYLES.values() for words in axes.values() for o in words.values() for k in o})
 
 
 def variants(algo: str) -> list:
-    """All option combinations of an algorithm's grid, default first."""
-    axes = AXES[algo]
-    names = list(axes)
-    return [dict(zip(names, combo)) for combo in itertools.product(*(axes[n] for n in names))]
+    """All style combinations of an algorithm, default first: a list of
+    (style words, kernel options)."""
+    axes = STYLES[algo]
+    out = []
+    for combo in itertools.product(*(list(axes[a].items()) for a in axes)):
+        words = [w for w, _ in combo]
+        opts = {}
+        for _, o in combo:
+            opts.update(o)
+        out.append((words, opts))
+    return out
 
 
-def variant_name(graph: str, algo: str, opts: dict) -> str:
-    style = "_".join(f"{LABEL[k]}{v}" for k, v in opts.items())
-    return f"{graph}_gb300_{algo.upper()}_GB300_{style}.cu"
+def variant_name(graph: str, algo: str, words: list) -> str:
+    return f"{graph}_gb300_{algo.upper()}_GB300_{'_'.join(words)}.cu"
 
 
 def write_csv(path: str, algo_rows: dict) -> None:
@@ -124,13 +166,13 @@ def result(algo, g, out, scores, cnt):
     return out.to_array(np.int32, g.nodes)
 
 
-def sweep(g, algos, repeat: int, graph_name: str, log=print) -> dict:
+def sweep(g, algos, repeat: int, graph_name: str, log=print, check=None) -> dict:
+    """Runs every variant of every algorithm; returns {algo: [(name, gteps)]}.
+    check(algo, words, result, iterations, graph) validates each variant's
+    result (default: equal to the first variant's; PageRank within 1e-6)."""
     gd = g.degree_ordered() if "tc" in algos else None
     src = int(g.pick_sources(1, seed=7)[0])
-    names = ("blocks_per_sm", "hub_degree", "bfs_alpha", "sssp_item_edges", "sssp_warp_degree", "sssp_window_scale",
-             "sssp_window_degree", "sssp_delta_scale", "sssp_heavy_split", "pr_blocks_per_sm", "pr_hub_degree",
-             "pr_chunk", "tc_block_chunk")
-    saved = {k: ig.get_option(k) for k in names}
+    saved = {k: ig.get_option(k) for k in OPTION_NAMES + ["bfs_beta"]}
     rows = {}
     with ig.DeviceCSR(g) as d:
         dd = ig.DeviceCSR(gd) if gd is not None else None
@@ -142,7 +184,7 @@ def sweep(g, algos, repeat: int, graph_name: str, log=print) -> dict:
             for algo in algos:
                 first = None
                 rows[algo] = []
-                for opts in variants(algo):
+                for words, opts in variants(algo):
                     for k, v in saved.items():
                         ig.set_option(k, v)
                     for k, v in opts.items():
@@ -158,18 +200,20 @@ def sweep(g, algos, repeat: int, graph_name: str, log=print) -> dict:
                     info = (GT if algo == "tc" else G).last_run()
                     ig.check(info.status)
                     r = result(algo, g, out, scores, cnt)
-                    if first is None:
+                    if check is not None:
+                        check(algo, words, r, info.iterations, gd if algo == "tc" else g, src)
+                    elif first is None:
                         first = r
                     elif algo == "pr":
                         rel = np.abs(r - first).sum() / np.abs(first).sum()
                         if rel > 1e-6:
-                            raise RuntimeError(f"{algo} variant {opts}: relative L1 {rel} from the first variant")
+                            raise RuntimeError(f"{algo} variant {words}: relative L1 {rel} from the first variant")
                     elif not np.array_equal(r, first):
-                        raise RuntimeError(f"{algo} variant {opts} changed the result")
+                        raise RuntimeError(f"{algo} variant {words} changed the result")
                     ms = float(np.median(times))
                     gteps = (gd.edges if algo == "tc" else g.edges) / (ms * 1e-3) / 1e9
-                    rows[algo].append((variant_name(graph_name, algo, opts), gteps))
-                    log(f"{algo} {opts}: median {ms:.3f} ms, {gteps:.3f} gigaedges/s")
+                    rows[algo].append((variant_name(graph_name, algo, words), gteps))
+                    log(f"{algo} {'_'.join(words)}: median {ms:.3f} ms, {gteps:.3f} gigaedges/s")
         finally:
             for k, v in saved.items():
                 ig.set_option(k, v)
@@ -191,7 +235,7 @@ def main():
     args = ap.parse_args()
     algos = [a for a in args.algos.split(",") if a]
     for a in algos:
-        if a not in AXES:
+        if a not in STYLES:
             raise SystemExit(f"unknown algorithm {a}")
     g = load_graph(args.graph)
     name = args.graph.replace(":", "").replace("/", "_")

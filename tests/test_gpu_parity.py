@@ -388,14 +388,24 @@ def test_traversal_option_forms_match_oracle(ig, orc, graphs, opt, values):
             ig.set_option(k, v)
 
 
-@pytest.mark.parametrize("subwarp,prefetch", [(1, 1), (0, 0)])
-def test_pagerank_gather_forms(ig, orc, graphs, subwarp, prefetch):
+@pytest.mark.parametrize("subwarp,prefetch,two", [(1, 1, 1), (0, 0, 0), (1, 0, 0), (0, 1, 1)])
+def test_pagerank_gather_forms(ig, orc, graphs, subwarp, prefetch, two):
     """Medium lists summed by 8-lane sub-warps or by the whole warp, with or
-    without the L2 prefetch: within 1e-6 relative L1 of FP64, deterministic."""
-    old = (ig.get_option("pr_subwarp"), ig.get_option("pr_prefetch"))
+    without the L2 prefetch, contributions gathered in a dense first pass or
+    while summing: within 1e-6 relative L1 of FP64, deterministic, and the
+    two-pass form gives the same bits as the one-pass form."""
+    old = (ig.get_option("pr_subwarp"), ig.get_option("pr_prefetch"), ig.get_option("pr_two_pass"))
     try:
         ig.set_option("pr_subwarp", subwarp)
         ig.set_option("pr_prefetch", prefetch)
+        ig.set_option("pr_two_pass", 1 - two)
+        other = {}
+        for name in ("rmat14", "hubby"):
+            g = graphs[name]
+            s = np.full(g.nodes, np.float32(1.0) / np.float32(g.nodes), np.float32)
+            ig.PR_GPU(g, s, g.degree(), 1e-6, 100)
+            other[name] = s
+        ig.set_option("pr_two_pass", two)
         for name in ("rmat14", "hubby", "er4k", "rmat18"):
             g = graphs[name]
             outs = []
@@ -404,8 +414,11 @@ def test_pagerank_gather_forms(ig, orc, graphs, subwarp, prefetch):
                 it, _ = ig.PR_GPU(g, s, g.degree(), 1e-6, 100)
                 outs.append(s)
             assert np.array_equal(outs[0], outs[1]), name
+            if name in other:
+                assert np.array_equal(outs[0], other[name]), name
             ref, _, _ = orc.pr_f64(g, iters=it)
             assert np.abs(outs[0] - ref).sum() / ref.sum() <= PR_TOL, name
     finally:
         ig.set_option("pr_subwarp", old[0])
         ig.set_option("pr_prefetch", old[1])
+        ig.set_option("pr_two_pass", old[2])

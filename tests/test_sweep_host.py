@@ -12,19 +12,33 @@ import sweep  # noqa: E402
 
 
 def test_first_variant_is_the_default(ig):
-    for algo, axes in sweep.AXES.items():
-        first = sweep.variants(algo)[0]
-        for name, value in first.items():
-            assert ig.get_option(name) == value, (algo, name)
+    """The first word of every axis sets nothing, so the first variant is the
+    library default; variants are the full product of the axes; every option
+    a style word sets exists and accepts its value."""
+    for algo, axes in sweep.STYLES.items():
+        words, opts = sweep.variants(algo)[0]
+        assert opts == {} and words == [next(iter(ax)) for ax in axes.values()]
         n = 1
         for vals in axes.values():
             n *= len(vals)
         assert len(sweep.variants(algo)) == n
+        for words, opts in sweep.variants(algo):
+            for name, value in opts.items():
+                old = ig.get_option(name)
+                ig.set_option(name, value)
+                ig.set_option(name, old)
+
+
+def test_style_words_name_the_axes():
+    names = [sweep.variant_name("rmat20", a, w) for a in sweep.STYLES for w, _ in sweep.variants(a)]
+    assert len(names) == len(set(names))
+    assert "rmat20_gb300_BFS_GB300_Pull_WarpGrid_Bitmap.cu" in names
+    assert "rmat20_gb300_SSSP_GB300_E_Window_Sync2_Plain.cu" in names
 
 
 def test_csv_round_trip(tmp_path):
-    rows = {"bfs": [(sweep.variant_name("rmat20", "bfs", {"blocks_per_sm": 4, "hub_degree": 256}), 12.5),
-                    (sweep.variant_name("rmat20", "bfs", {"blocks_per_sm": 2, "hub_degree": 64}), 3.25)]}
+    rows = {"bfs": [(sweep.variant_name("rmat20", "bfs", ["PushPull", "WarpGrid", "Bitmap"]), 12.5),
+                    (sweep.variant_name("rmat20", "bfs", ["Push", "Warp", "Dist"]), 3.25)]}
     p = tmp_path / "t.csv"
     sweep.write_csv(str(p), rows)
     text = p.read_text()
