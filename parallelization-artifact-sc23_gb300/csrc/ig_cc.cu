@@ -233,7 +233,11 @@ int igk_cc(IgExec* ex, const ig_csr* dg, int* d_label, bool sample) {
   const int grid_v = std::min((n + kThreads - 1) / kThreads, ex->sms * 16);
   const int grid_w = std::max(1, std::min((n + kThreads - 1) / kThreads, ex->sms * 8));
   cc_init<<<grid_v, kThreads, 0, ex->stream>>>(dg->nindex, dg->nlist, n, d_label);
-  if (sample && o.cc_rounds) {
+  if (sample && o.cc_rounds == 2) {  // the init forest flattened before the sampled unions
+    cc_compress<<<grid_v, kThreads, 0, ex->stream>>>(d_label, n);
+    ig_count_launches(1);
+  }
+  if (sample && o.cc_rounds == 1) {
     // neighbour r of every vertex linked in its own round, trees flattened after each
     for (int r = 0; r < kSample; r++) {
       cc_link_round<<<grid_v, kThreads, 0, ex->stream>>>(dg->nindex, dg->nlist, n, d_label, r);

@@ -27,7 +27,8 @@ struct IgOptions {
                           // dense pass (128-bit loads and stores), then sums the lists from it
   int tc_block_chunk;     // TC: in-neighbours per block work item
   int cc_rounds;          // CC: 1 = sampled neighbours linked one round at a time (read-only root
-                          // searches, a compression after each), 0 = both in one pass with path halving
+                          // searches, a compression after each), 0 = both in one pass with path
+                          // halving, 2 = as 0 after flattening the initial forest
 };
 
 IgOptions& ig_options();
