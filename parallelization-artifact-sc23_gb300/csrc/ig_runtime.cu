@@ -669,7 +669,7 @@ IgOptions& ig_options() {
       /*pr_blocks_per_sm=*/4,
       /*pr_prefetch=*/1,
       /*pr_subwarp=*/1,
-      /*pr_two_pass=*/1,
+      /*pr_two_pass=*/0,
       /*tc_block_chunk=*/4096,
       /*cc_rounds=*/0,
   };

@@ -52,10 +52,12 @@ BIG = 1 << 30
 #        Plain / LightHeavy edge split.  (Always a data-driven worklist.)
 #   CC   link: Pass = sampled neighbours linked in one pass with path
 #        halving, Rounds = one round per neighbour with a compression after
-#        each; granularity as BFS.  (Hooking pushes along edges.)
+#        each, FlatPass = Pass after flattening the initial forest;
+#        granularity as BFS.  (Hooking pushes along edges.)
 #   MIS  residency only (B4 / B2 / B8 blocks per SM).
-#   PR   gather: TwoPass = every edge's contribution gathered first in one
-#        dense pass, OnePass = gathered while summing; granularity: SubWarp =
+#   PR   gather: OnePass = contributions gathered while summing, TwoPass =
+#        every edge's contribution gathered first in one dense pass (measured
+#        slower: the gathers cost the same either way); granularity: SubWarp =
 #        medium lists four at a time by 8-lane sub-warps, WarpPair = by the
 #        whole warp two at a time; hub chunks of 1024 /
 #        4096 / 256 edges; Prefetch / NoPrefetch of each warp's next lists.
@@ -69,10 +71,10 @@ STYLES = {
              "order": {"Window": {}, "NoWindow": {"sssp_window_scale": 0}},
              "sync": {"Sync2": {}, "Sync1": {"sssp_merge_below": BIG}},
              "split": {"Plain": {}, "LightHeavy": {"sssp_heavy_split": 1}}},
-    "cc": {"link": {"Pass": {}, "Rounds": {"cc_rounds": 1}},
+    "cc": {"link": {"Pass": {}, "Rounds": {"cc_rounds": 1}, "FlatPass": {"cc_rounds": 2}},
            "granularity": {"WarpGrid": {}, "Grid": {"hub_degree": 64}, "Warp": {"hub_degree": BIG}}},
     "mis": {"residency": {"B4": {}, "B2": {"blocks_per_sm": 2}, "B8": {"blocks_per_sm": 8}}},
-    "pr": {"gather": {"TwoPass": {}, "OnePass": {"pr_two_pass": 0}},
+    "pr": {"gather": {"OnePass": {}, "TwoPass": {"pr_two_pass": 1}},
            "granularity": {"SubWarp": {}, "WarpPair": {"pr_subwarp": 0}},
            "hubs": {"Chunk1024": {}, "Chunk4096": {"pr_hub_degree": 4096}, "Chunk256": {"pr_hub_degree": 256}},
            "prefetch": {"Prefetch": {}, "NoPrefetch": {"pr_prefetch": 0}}},

@@ -127,6 +127,7 @@ def test_autotune_keeps_results(ig, gpu, expected):
         assert b.get_option("pr", "pr_hub_degree") in (ig.get_option("pr_hub_degree"), 1024, 4096)
         assert b.get_option("pr", "pr_blocks_per_sm") in (ig.get_option("pr_blocks_per_sm"), 3, 4)
         assert b.get_option("pr", "pr_subwarp") in (0, 1)
+        same_pr_form = all(b.get_option("pr", k) == ig.get_option(k) for k in ("pr_subwarp", "pr_two_pass"))
         outs = run_batch(ig, b)
     for call, (dist, lab, cnt, sc, its) in enumerate(outs):
         for i, (e_dist, e_lab, e_tc, e_sc, e_it) in enumerate(expected):
@@ -138,7 +139,7 @@ def test_autotune_keeps_results(ig, gpu, expected):
             # within tolerance, and the same bits when it kept the warp form
             s_ = sc[v0:v1].astype(np.float64)
             assert np.abs(s_ - e_sc).sum() / e_sc.sum() <= 1e-6 and abs(int(its[i]) - e_it) <= 1, (call, i, "pr")
-            if b.get_option("pr", "pr_subwarp") == ig.get_option("pr_subwarp"):
+            if same_pr_form:
                 assert int(its[i]) == e_it and np.array_equal(sc[v0:v1], e_sc), (call, i, "pr bits")
 
 
