@@ -256,6 +256,15 @@ def run_ours(args, dist: Dist):
                   "max_ms": round(float(cm.max()), 4), "gteps": round(E / (ms_call * 1e-3) / 1e9, 3),
                   "algorithmic_bytes": abytes[k], "achieved_gbs": round(gbs, 1),
                   "hbm_frac": round(gbs / peaks["hbm_gbs"], 4)}
+        if k in DRAM_BYTES_PER_CALL:  # what DRAM actually moved (capture, scaled), per unit of this call's time
+            dg = DRAM_BYTES_PER_CALL[k] / (ms_call * 1e-3) / 1e9
+            per[k].update({"dram_bytes_per_call": DRAM_BYTES_PER_CALL[k], "dram_gbs": round(dg, 1),
+                           "dram_frac": round(dg / peaks["hbm_gbs"], 4)})
+    # The triangle-count formula counts every intersection read once, but the
+    # exact-bitmap kernel serves one side of each probe from shared memory:
+    # its "achieved" can exceed the copy peak.  dram_frac is the DRAM figure.
+    per["tc"]["hbm_frac_note"] = ("algorithmic bytes count probe reads served from shared memory; "
+                                  "dram_frac is what DRAM moved")
     per["pr"]["iterations"] = pr_iters
     shares = {k: acc[k] / max(1e-9, sum(acc.values())) for k in ALGOS}
     dom = max(shares, key=shares.get)
@@ -476,12 +485,17 @@ def load_peaks() -> dict:
     return {"hbm_gbs": 6800.0, "source": "fallback 6.8 TB/s"}
 
 
-# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per call of the
-# dominant algorithm's kernel on this workload, from one ncu capture of that
-# kernel alone on RMAT-21 scaled to RMAT-22 by edges processed; the capture
-# command and the figures are recorded beside the kernel's profile summary.
-# None where no capture of the current kernel exists.
-DRAM_BYTES_PER_CALL = {}
+# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per call of each
+# algorithm's main kernel on this workload: one ncu capture of that kernel
+# alone (-k, -c 2) on the RMAT scale-21 case (`bench.py --case <algo> --scale
+# 21`: 63,539,260 edges), scaled to RMAT-22 by the edge ratio 2.019 (the
+# traffic grows with the edges processed).  Kernels: sssp_persistent,
+# pr_persistent (15 iterations), tc_count_block (exact and hashed forms; the
+# orientation kernels are not included), bfs_persistent, mis_persistent,
+# cc_sample (CC's largest kernel).  The capture and its figures are in the
+# per-kernel traffic summary under profiles/.
+DRAM_BYTES_PER_CALL = {"sssp": 2497888874, "pr": 9041198075, "tc": 4028693498, "bfs": 155368847,
+                       "mis": 167385116, "cc": 148094672}
 
 
 # ----------------------------------------------------------------------------- CPU
