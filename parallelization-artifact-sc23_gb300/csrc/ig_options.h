@@ -18,6 +18,8 @@ struct IgOptions {
   int sssp_merge_below;   // SSSP: a round whose frontier is below this expands (up to 65,536 of) its
                           // work items without a second grid barrier (0 = never)
   int sssp_spin_ns;       // SSSP: pause between polls of a warp waiting for work items (merged rounds)
+  int sssp_pair_slices;   // SSSP: work-item slices expanded two at a time (eight edges per lane):
+                          // 1 = at 3 blocks per SM, 2 = at 4 (register spills); 0 = one at a time
   int pr_hub_degree;      // PageRank: degree above which a vertex is split in chunks
   int pr_chunk;           // PageRank: edges per hub chunk
   int pr_blocks_per_sm;   // PageRank: resident blocks per SM (0 = blocks_per_sm)

@@ -30,6 +30,8 @@
 // pending distance mf is found, T becomes max(T, mf) + delta, entries below the
 // old T are stale (already settled through the near queue) and dropped,
 // entries below the new T form the next near queue, the rest stay far.
+#include <type_traits>
+
 #include "ig_device.cuh"
 #include "ig_options.h"
 
@@ -38,6 +40,7 @@ namespace {
 constexpr int kThreads = 256;
 constexpr int kDeltaSamples = 4096;
 constexpr int kSlice = 128;  // edges of a work-item slice: four per lane of one warp
+constexpr int kQBuf = 32 + 32 * 8;  // warp staging: 32 + the most one step adds (two slices, 8 per lane)
 static_assert(kSlice == 4 * 32, "a slice is one relax4 step of a warp");
 
 struct SsspArgs {
@@ -108,7 +111,7 @@ __device__ __forceinline__ void publish_min(int& v, int* slot) {
   v = ig::kInf;
 }
 
-template <int kMinBlocks>
+template <int kMinBlocks, bool kPair>
 __global__ void __launch_bounds__(kThreads, kMinBlocks) sssp_persistent(SsspArgs a) {
   using namespace ig;
   IgCtl* ctl = a.ctl;
@@ -119,7 +122,7 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) sssp_persistent(SsspArgs
   const long long gthreads = (long long)gridDim.x * blockDim.x;
   const int warp_g = (int)(gtid >> 5);
   const int nwarps = (int)(gthreads >> 5);
-  __shared__ int s_qbuf[kThreads / 32][2][kWarpBuf];  // per-warp staging of near / far appends
+  __shared__ int s_qbuf[kThreads / 32][2][kPair ? kQBuf : kWarpBuf];  // per-warp staging of near / far appends
   int* nbuf = s_qbuf[threadIdx.x >> 5][0];
   int* fbuf = s_qbuf[threadIdx.x >> 5][1];
   int nbuf_n = 0, fbuf_n = 0;
@@ -224,11 +227,12 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) sssp_persistent(SsspArgs
       // atomic.  Another edge may have lowered the distance further in the
       // meantime; the vertex is then queued once more than needed (the stamp
       // keeps it to one entry per queue, the expanded-distance check skips it).
-      auto relax4 = [&](const bool (&act)[4], const int (&e)[4], const int (&du)[4]) {
-        int v[4], w[4], dv[4], sv[4];
-        bool cand[4];
+      auto relax4 = [&](const auto& act, const auto& e, const auto& du) {
+        constexpr int N = std::extent<std::remove_reference_t<decltype(act)>>::value;  // 4, or 8 for two slices
+        int v[N], w[N], dv[N], sv[N];
+        bool cand[N];
 #pragma unroll
-        for (int k = 0; k < 4; k++) {
+        for (int k = 0; k < N; k++) {
           v[k] = 0;
           w[k] = 0;
           if (act[k] && du[k] != kInf) {
@@ -237,18 +241,18 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) sssp_persistent(SsspArgs
           }
         }
 #pragma unroll
-        for (int k = 0; k < 4; k++) dv[k] = (act[k] && du[k] != kInf) ? a.dist[v[k]] : 0;
+        for (int k = 0; k < N; k++) dv[k] = (act[k] && du[k] != kInf) ? a.dist[v[k]] : 0;
 #pragma unroll
-        for (int k = 0; k < 4; k++) {
+        for (int k = 0; k < N; k++) {
           const bool light = !a.heavy_split || (long long)w[k] < delta;
           cand[k] = act[k] && du[k] != kInf && light != heavy && (long long)du[k] + w[k] < (long long)dv[k];
           if (cand[k]) atomicMin(&a.dist[v[k]], du[k] + w[k]);
         }
 #pragma unroll
-        for (int k = 0; k < 4; k++) sv[k] = cand[k] ? a.stamp[v[k]] : 0;
-        bool tn[4], tf[4];
+        for (int k = 0; k < N; k++) sv[k] = cand[k] ? a.stamp[v[k]] : 0;
+        bool tn[N], tf[N];
 #pragma unroll
-        for (int k = 0; k < 4; k++) {
+        for (int k = 0; k < N; k++) {
           tn[k] = tf[k] = false;
           if (cand[k]) {
             improved++;
@@ -261,7 +265,7 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) sssp_persistent(SsspArgs
             }
           }
         }
-        warp_buf_append2_flags<4>(v, tn, nbuf, nbuf_n, nxt, qsize, tf, fbuf, fbuf_n, far, fsize, a.nodes, ctl);
+        warp_buf_append2_flags<N>(v, tn, nbuf, nbuf_n, nxt, qsize, tf, fbuf, fbuf_n, far, fsize, a.nodes, ctl);
       };
       // first chunk by warp index, the rest taken from a per-round counter so
       // that warps that drew light chunks take more (the round ends at the
@@ -376,14 +380,13 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) sssp_persistent(SsspArgs
       // (no owner search); expand_slices runs slices j0..j1-1 of the items
       // whose headers lanes 0.. hold (item mfirst + t in lane t).
       auto expand_slices = [&](long long j0, long long j1, int mfirst, int hdu, int hb, int hd) {
-        for (long long j = j0; j < j1; j++) {
+        // slice j's four edges per lane into act/e/duk[o, o + 4)
+        auto slice_edges = [&](long long j, bool* act, int* e, int* duk) {
           const int t = (int)(j >> slog) - mfirst;
           const int du = __shfl_sync(IG_FULL, hdu, t);
           const int b = __shfl_sync(IG_FULL, hb, t);
           const int d = __shfl_sync(IG_FULL, hd, t);
           const int s0 = (int)(j & ((1LL << slog) - 1)) * kSlice;
-          bool act[4];
-          int e[4], duk[4];
 #pragma unroll
           for (int k = 0; k < 4; k++) {
             const int off = s0 + k * 32 + lane;
@@ -391,6 +394,20 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) sssp_persistent(SsspArgs
             e[k] = b + (act[k] ? off : 0);
             duk[k] = du;
           }
+        };
+        long long j = j0;
+        if (kPair)  // two slices per step: eight edges per lane, their loads issued together
+          for (; j + 1 < j1; j += 2) {
+            bool act[8];
+            int e[8], duk[8];
+            slice_edges(j, act, e, duk);
+            slice_edges(j + 1, act + 4, e + 4, duk + 4);
+            relax4(act, e, duk);
+          }
+        for (; j < j1; j++) {
+          bool act[4];
+          int e[4], duk[4];
+          slice_edges(j, act, e, duk);
           relax4(act, e, duk);
         }
       };
@@ -625,8 +642,11 @@ int igk_sssp(IgExec* ex, const ig_csr* dg, int src, int* d_dist) {
              o.sssp_window_degree, o.sssp_merge_below, o.sssp_spin_ns};
   void* args[] = {&a};
   // the register budget follows the residency cap (4, 5 or 6 blocks of 256 threads per SM)
-  const void* kern = o.blocks_per_sm >= 6 || o.blocks_per_sm == 0 ? (const void*)sssp_persistent<6>
-                     : o.blocks_per_sm == 5                        ? (const void*)sssp_persistent<5>
-                                                                   : (const void*)sssp_persistent<4>;
+  // (the paired-slice form holds more registers: 3 blocks per SM, or 4 with spills)
+  const void* kern = o.sssp_pair_slices == 2                        ? (const void*)sssp_persistent<4, true>
+                     : o.sssp_pair_slices                          ? (const void*)sssp_persistent<3, true>
+                     : o.blocks_per_sm >= 6 || o.blocks_per_sm == 0 ? (const void*)sssp_persistent<6, false>
+                     : o.blocks_per_sm == 5                        ? (const void*)sssp_persistent<5, false>
+                                                                   : (const void*)sssp_persistent<4, false>;
   return ig_launch_coop(ex, kern, kThreads, 0, o.blocks_per_sm, args, nullptr);
 }

@@ -422,3 +422,25 @@ def test_pagerank_gather_forms(ig, orc, graphs, subwarp, prefetch, two):
         ig.set_option("pr_subwarp", old[0])
         ig.set_option("pr_prefetch", old[1])
         ig.set_option("pr_two_pass", old[2])
+
+
+@pytest.mark.parametrize("pair", [1, 2])
+def test_sssp_paired_slices(ig, orc, graphs, pair):
+    """Work-item slices expanded two at a time (eight edges per lane, at 3 or
+    4 resident blocks per SM): exact distances, with lists of every length
+    cut into items (item threshold 4) and with the default threshold."""
+    old = {k: ig.get_option(k) for k in ("sssp_pair_slices", "sssp_warp_degree")}
+    try:
+        ig.set_option("sssp_pair_slices", pair)
+        for wd in (64, 4):
+            ig.set_option("sssp_warp_degree", wd)
+            for name in ("rmat14", "hubby", "road128", "star", "rmat18"):
+                g = graphs[name]
+                with ig.DeviceCSR(g) as d:
+                    for s in (0, g.nodes // 2):
+                        dist = np.empty(g.nodes, np.int32)
+                        ig.GPUsssp_vertex(int(s), d, dist)
+                        assert np.array_equal(dist, orc.sssp(g, int(s))), (name, s, wd)
+    finally:
+        for k, v in old.items():
+            ig.set_option(k, v)
