@@ -311,8 +311,8 @@ def run_ours(args, dist: Dist):
         sv = run_served(args, dist)
         forms = {
             "batched": {k: bt[k] for k in ("metric", "value", "unit", "ms_per_step", "scaling", "config",
-                                           "per_algo_ms", "pr_iterations_per_graph", "plain", "speedup_vs_plain",
-                                           "clocks", "gpu_launches")},
+                                           "per_algo_ms", "pr_iterations_per_graph", "autotuned", "plain",
+                                           "speedup_vs_plain", "clocks", "gpu_launches")},
             "served": {k: sv[k] for k in ("metric", "value", "unit", "config", "per_kind", "clocks")},
         }
     out = {
@@ -725,9 +725,7 @@ def run_batched(args, dist: Dist, graphs: int = BATCH_GRAPHS):
     if not args.no_autotune:
         t1 = time.time()
         tune_ms = b.autotune(("bfs", "cc", "pr"), reps=2)
-        tuned = {a: {"ms": round(tune_ms[a], 3),
-                     "options": {k: b.get_option(a, k) for k in ("blocks_per_sm", "hub_degree", "pr_hub_degree",
-                                                                  "pr_blocks_per_sm")}}
+        tuned = {a: {"ms": round(tune_ms[a], 3), "options": {k: b.get_option(a, k) for k in ig.Batch.TUNED[a]}}
                  for a in tune_ms}
         log(f"[bench] autotuned in {time.time() - t1:.1f}s: {tuned}")
     for _ in range(args.warmup):

@@ -255,7 +255,7 @@ std::vector<IgOptions> batch_variants(int algo, const IgOptions& base) {
   // (data-driven worklist levels) and bitmap against distance tests in the
   // bottom-up (pull, topology-driven) levels; CC sampled linking in one pass
   // or one round per neighbour; PageRank medium lists by the warp or by
-  // 8-lane sub-warps.
+  // 8-lane sub-warps, with or without the L2 prefetch of the next lists.
   if (algo == kBfs) {
     for (int bps : {4, 8})
       for (int hub : {256, 1024})
@@ -274,10 +274,12 @@ std::vector<IgOptions> batch_variants(int algo, const IgOptions& base) {
   } else if (algo == kPr) {
     for (int bps : {3, 4})
       for (int ph : {1024, 4096})
-        for (int sub : {0, 1}) {
-          add(bps, 0, ph);
-          out.back().pr_subwarp = sub;
-        }
+        for (int sub : {0, 1})
+          for (int pf : {1, 0}) {
+            add(bps, 0, ph);
+            out.back().pr_subwarp = sub;
+            out.back().pr_prefetch = pf;
+          }
   }
   return out;  // TC: its launch shape follows the shared-memory tables; nothing to tune
 }

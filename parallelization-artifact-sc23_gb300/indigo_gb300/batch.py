@@ -122,7 +122,7 @@ class Batch:
     TUNED = {"bfs": ("blocks_per_sm", "hub_degree", "bfs_alpha", "bfs_bitmap"),
              "cc": ("hub_degree", "cc_rounds"),
              "tc": (),
-             "pr": ("pr_blocks_per_sm", "pr_hub_degree", "pr_subwarp")}
+             "pr": ("pr_blocks_per_sm", "pr_hub_degree", "pr_subwarp", "pr_prefetch")}
 
     def stats_key(self) -> str:
         """The tuning database's key for this batch: log2 buckets of the graph
