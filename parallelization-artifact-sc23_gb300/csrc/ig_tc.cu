@@ -470,11 +470,12 @@ __global__ void __launch_bounds__(kThreads, 8) tc_count_block(const int* __restr
                                                               const int* __restrict__ item_v, int n,
                                                               unsigned long long* count, const IgCtl* ctl,
                                                               const int* __restrict__ graph_vptr, int graphs,
-                                                              int block_chunk) {
+                                                              int block_chunk, int grab, int* grab_ctr) {
   using namespace ig;
   // the exact bitmap, or the hash table followed by the filter
   __shared__ unsigned s_mem[kExact ? kSpanWords : kHashCap + kBitWords];
   __shared__ int s_next;
+  __shared__ int s_run;
   int* tab = (int*)s_mem;
   unsigned* bits = s_mem + kHashCap;
   if (ctl->err) return;
@@ -485,7 +486,18 @@ __global__ void __launch_bounds__(kThreads, 8) tc_count_block(const int* __restr
   int cur_v = -1;
   unsigned mask = 0;
   bool hashed = false;
-  for (int it = blockIdx.x; it < items; it += gridDim.x) {
+  // Items are taken one per block in a grid stride, or (grab > 0) in runs of
+  // `grab` consecutive items from a counter, so that the items of one middle
+  // vertex mostly stay in one block and its table is built once.
+  auto next_run = [&](int cur) {
+    if (grab <= 0) return cur < 0 ? (int)blockIdx.x : cur + (int)gridDim.x;
+    __syncthreads();
+    if (threadIdx.x == 0) s_run = atomicAdd(grab_ctr, grab);
+    __syncthreads();
+    return s_run;
+  };
+  for (int run = next_run(-1); run < items; run = next_run(run))
+  for (int it = run; it < (grab > 0 ? min(run + grab, items) : run + 1); it++) {
     const int v = __ldg(&item_v[it]);  // middle vertex (block-uniform)
     const int span = n - 1 - v;        // ids above v
     if ((ranked && span <= kSpanWords * 32) != kExact) continue;  // the other launch's item
@@ -564,6 +576,7 @@ static int tc_run(IgExec* ex, int nodes, int edges, const int* d_nindex, const i
                   const int* d_graph_vptr, int graphs) {
   const size_t vb = ((size_t)nodes + 1) * sizeof(int);
   const int block_chunk = ig_exec_options(ex).tc_block_chunk;
+  const int grab = ig_exec_options(ex).tc_grab;
   void *cnt, *off, *icnt, *ioff, *icnt_b, *ioff_b, *list, *inl, *hubs, *itemv, *itemv_b;
   int rc;
   if ((rc = ig_scratch_get(ex->scratch, IG_SLOT_V0, vb, &cnt))) return rc;
@@ -609,20 +622,20 @@ static int tc_run(IgExec* ex, int nodes, int edges, const int* d_nindex, const i
   if (d_graph_vptr) {
     tc_count_block<true, true><<<cgrid, kThreads, 0, ex->stream>>>(
         (const int*)off, (const int*)list, d_nindex, (const int*)inl, (const int*)ioff_b, (const int*)itemv_b, nodes,
-        d_count, ex->d_ctl, d_graph_vptr, graphs, block_chunk);
+        d_count, ex->d_ctl, d_graph_vptr, graphs, block_chunk, grab, &ex->d_ctl->hot[0]);
     tc_count_block<true, false><<<cgrid, kThreads, 0, ex->stream>>>(
         (const int*)off, (const int*)list, d_nindex, (const int*)inl, (const int*)ioff_b, (const int*)itemv_b, nodes,
-        d_count, ex->d_ctl, d_graph_vptr, graphs, block_chunk);
+        d_count, ex->d_ctl, d_graph_vptr, graphs, block_chunk, grab, &ex->d_ctl->hot[kCtlSpread]);
     tc_count_warp<true><<<cgrid, kThreads, 0, ex->stream>>>((const int*)off, (const int*)list, d_nindex,
                                                             (const int*)inl, (const int*)ioff, (const int*)itemv,
                                                             nodes, d_count, ex->d_ctl, d_graph_vptr, graphs);
   } else {
     tc_count_block<false, true><<<cgrid, kThreads, 0, ex->stream>>>(
         (const int*)off, (const int*)list, d_nindex, (const int*)inl, (const int*)ioff_b, (const int*)itemv_b, nodes,
-        d_count, ex->d_ctl, nullptr, 0, block_chunk);
+        d_count, ex->d_ctl, nullptr, 0, block_chunk, grab, &ex->d_ctl->hot[0]);
     tc_count_block<false, false><<<cgrid, kThreads, 0, ex->stream>>>(
         (const int*)off, (const int*)list, d_nindex, (const int*)inl, (const int*)ioff_b, (const int*)itemv_b, nodes,
-        d_count, ex->d_ctl, nullptr, 0, block_chunk);
+        d_count, ex->d_ctl, nullptr, 0, block_chunk, grab, &ex->d_ctl->hot[kCtlSpread]);
     tc_count_warp<false><<<cgrid, kThreads, 0, ex->stream>>>((const int*)off, (const int*)list, d_nindex,
                                                              (const int*)inl, (const int*)ioff, (const int*)itemv,
                                                              nodes, d_count, ex->d_ctl, nullptr, 0);

@@ -62,7 +62,8 @@ BIG = 1 << 30
 #        whole warp two at a time; hub chunks of 1024 /
 #        4096 / 256 edges; Prefetch / NoPrefetch of each warp's next lists.
 #        (Pull only: push PageRank needs float atomics, not deterministic.)
-#   TC   block work items of 4096 / 1024 in-neighbours.
+#   TC   block work items of 4096 / 1024 in-neighbours, dealt to blocks in a
+#        grid stride or taken in runs of 4 from a counter.
 STYLES = {
     "bfs": {"direction": {"PushPull": {}, "Push": {"bfs_alpha": 0}, "Pull": {"bfs_alpha": 1000000}},
             "granularity": {"WarpGrid": {}, "Warp": {"hub_degree": BIG}, "Grid": {"hub_degree": 32}},
@@ -78,7 +79,8 @@ STYLES = {
            "granularity": {"SubWarp": {}, "WarpPair": {"pr_subwarp": 0}},
            "hubs": {"Chunk1024": {}, "Chunk4096": {"pr_hub_degree": 4096}, "Chunk256": {"pr_hub_degree": 256}},
            "prefetch": {"Prefetch": {}, "NoPrefetch": {"pr_prefetch": 0}}},
-    "tc": {"items": {"Item4096": {}, "Item1024": {"tc_block_chunk": 1024}}},
+    "tc": {"items": {"Item4096": {}, "Item1024": {"tc_block_chunk": 1024}},
+           "schedule": {"Stride": {}, "Runs4": {"tc_grab": 4}}},
 }
 AXES = STYLES  # the per-algorithm axes (name kept for callers)
 OPTION_NAMES = sorted({k for axes in STYLES.values() for words in axes.values() for o in words.values() for k in o})

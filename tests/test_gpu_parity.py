@@ -444,3 +444,20 @@ def test_sssp_paired_slices(ig, orc, graphs, pair):
     finally:
         for k, v in old.items():
             ig.set_option(k, v)
+
+
+@pytest.mark.parametrize("grab", [1, 4, 16])
+def test_tc_item_runs(ig, orc, graphs, grab):
+    """Block work items taken in runs from a counter instead of a grid
+    stride: the same counts, on the plain and the degree-ordered ids."""
+    old = (ig.get_option("tc_grab"), ig.get_option("tc_block_chunk"))
+    try:
+        ig.set_option("tc_grab", grab)
+        ig.set_option("tc_block_chunk", 256)  # many items per middle vertex
+        for name in ("rmat14", "hubby", "complete", "rmat18"):
+            for g in (graphs[name], graphs[name].degree_ordered()):
+                with ig.DeviceCSR(g) as d:
+                    assert ig.GPUtc_vertex(g.nodes, d.nindex_ptr, d.nlist_ptr)[0] == orc.tc(g), (name, grab)
+    finally:
+        ig.set_option("tc_grab", old[0])
+        ig.set_option("tc_block_chunk", old[1])
