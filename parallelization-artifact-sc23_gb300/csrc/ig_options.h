@@ -28,7 +28,8 @@ struct IgOptions {
   int pr_two_pass;        // PageRank: 1 = each iteration first gathers every edge's contribution in one
                           // dense pass (128-bit loads and stores), then sums the lists from it
   int tc_block_chunk;     // TC: in-neighbours per block work item
-  int tc_grab;            // TC: block work items taken in runs of this many from a counter (0: grid stride)
+  int tc_grab;            // TC: block work items taken in runs of this many from a counter, so a middle
+                          // vertex's items mostly share one block and its table (0: grid stride)
   int cc_rounds;          // CC: 1 = sampled neighbours linked one round at a time (read-only root
                           // searches, a compression after each), 0 = both in one pass with path
                           // halving, 2 = as 0 after flattening the initial forest

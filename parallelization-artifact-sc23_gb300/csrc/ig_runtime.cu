@@ -669,10 +669,10 @@ IgOptions& ig_options() {
       /*pr_chunk=*/4096,
       /*pr_blocks_per_sm=*/4,
       /*pr_prefetch=*/1,
-      /*pr_subwarp=*/1,
+      /*pr_subwarp=*/0,
       /*pr_two_pass=*/0,
       /*tc_block_chunk=*/4096,
-      /*tc_grab=*/0,
+      /*tc_grab=*/2,
       /*cc_rounds=*/0,
   };
   return o;

@@ -28,7 +28,10 @@
 //               halved when the ids are already in (degree, id) order (the
 //               degree-ordered input of the benchmark): then only the part
 //               of N+(u) after v is scanned.  The filter rejects most misses
-//               before the hash probe.
+//               before the hash probe.  Blocks take their work items in runs
+//               of consecutive items from a counter, so the items of one
+//               middle vertex usually share a block and its table or bitmap
+//               is built once.
 #include "ig_device.cuh"
 #include "ig_options.h"
 

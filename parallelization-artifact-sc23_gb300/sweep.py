@@ -57,13 +57,13 @@ BIG = 1 << 30
 #   MIS  residency only (B4 / B2 / B8 blocks per SM).
 #   PR   gather: OnePass = contributions gathered while summing, TwoPass =
 #        every edge's contribution gathered first in one dense pass (measured
-#        slower: the gathers cost the same either way); granularity: SubWarp =
-#        medium lists four at a time by 8-lane sub-warps, WarpPair = by the
-#        whole warp two at a time; hub chunks of 1024 /
+#        slower: the gathers cost the same either way); granularity: WarpPair
+#        = medium lists by the whole warp two at a time, SubWarp = four at a
+#        time by 8-lane sub-warps; hub chunks of 1024 /
 #        4096 / 256 edges; Prefetch / NoPrefetch of each warp's next lists.
 #        (Pull only: push PageRank needs float atomics, not deterministic.)
-#   TC   block work items of 4096 / 1024 in-neighbours, dealt to blocks in a
-#        grid stride or taken in runs of 4 from a counter.
+#   TC   block work items of 4096 / 1024 in-neighbours, taken by blocks in
+#        runs of 2 or 4 from a counter or dealt in a grid stride.
 STYLES = {
     "bfs": {"direction": {"PushPull": {}, "Push": {"bfs_alpha": 0}, "Pull": {"bfs_alpha": 1000000}},
             "granularity": {"WarpGrid": {}, "Warp": {"hub_degree": BIG}, "Grid": {"hub_degree": 32}},
@@ -76,11 +76,11 @@ STYLES = {
            "granularity": {"WarpGrid": {}, "Grid": {"hub_degree": 64}, "Warp": {"hub_degree": BIG}}},
     "mis": {"residency": {"B4": {}, "B2": {"blocks_per_sm": 2}, "B8": {"blocks_per_sm": 8}}},
     "pr": {"gather": {"OnePass": {}, "TwoPass": {"pr_two_pass": 1}},
-           "granularity": {"SubWarp": {}, "WarpPair": {"pr_subwarp": 0}},
+           "granularity": {"WarpPair": {}, "SubWarp": {"pr_subwarp": 1}},
            "hubs": {"Chunk1024": {}, "Chunk4096": {"pr_hub_degree": 4096}, "Chunk256": {"pr_hub_degree": 256}},
            "prefetch": {"Prefetch": {}, "NoPrefetch": {"pr_prefetch": 0}}},
     "tc": {"items": {"Item4096": {}, "Item1024": {"tc_block_chunk": 1024}},
-           "schedule": {"Stride": {}, "Runs4": {"tc_grab": 4}}},
+           "schedule": {"Runs2": {}, "Stride": {"tc_grab": 0}, "Runs4": {"tc_grab": 4}}},
 }
 AXES = STYLES  # the per-algorithm axes (name kept for callers)
 OPTION_NAMES = sorted({k for axes in STYLES.values() for words in axes.values() for o in words.values() for k in o})
