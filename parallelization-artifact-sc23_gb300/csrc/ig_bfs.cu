@@ -47,13 +47,17 @@ struct BfsArgs {
   // bottom-up scan tests a neighbour's bit instead of reading its distance.
   // Null: the scan reads distances (the allocation-free entry point).
   unsigned* bits;
+  // when set, the source is read from the device: the vertex encoded in the
+  // low word of *src_key as 0xffffffff - id (connected components' seed)
+  const unsigned long long* src_key;
 };
 
 // Hot counters of the control block, slot s = level % 3: hot32(s) size of the
 // queue built during the level, hot32(3 + s) its hub count, hot64(6 + s) the
 // sum of degrees of the queued vertices.
 
-__global__ void __launch_bounds__(kThreads) bfs_persistent(BfsArgs a) {
+__global__ void __launch_bounds__(kThreads) bfs_persistent(BfsArgs a_in) {
+  BfsArgs a = a_in;
   using namespace ig;
   IgCtl* ctl = a.ctl;
   const int lane = lane_id();
@@ -61,6 +65,7 @@ __global__ void __launch_bounds__(kThreads) bfs_persistent(BfsArgs a) {
   const long long gthreads = (long long)gridDim.x * blockDim.x;
   const int warp_g = (int)(gtid >> 5);
   const int nwarps = (int)(gthreads >> 5);
+  if (a.src_key) a.src = (int)(0xffffffffu - (unsigned)(*a.src_key & 0xffffffffull));
   const long long nwords = ((long long)a.nodes + 31) >> 5;
   if (a.bits)  // all three level bitmaps start empty but for a single source's bit
     for (long long i = gtid; i < 3 * nwords; i += gthreads)
@@ -216,7 +221,27 @@ int igk_bfs(IgExec* ex, const ig_csr* dg, int src, int* d_dist) {
   const IgOptions& o = ig_exec_options(ex);
   BfsArgs a{dg->nindex, dg->nlist, dg->nodes, dg->edges, src, d_dist, (int*)qa, (int*)qb, (int*)hubs,
             ex->d_ctl, ex->timeout_ns, o.hub_degree, o.bfs_alpha, o.bfs_beta, nullptr, 0,
-            o.bfs_bitmap ? (unsigned*)bits : nullptr};
+            o.bfs_bitmap ? (unsigned*)bits : nullptr, nullptr};
+  void* args[] = {&a};
+  return ig_launch_coop(ex, (const void*)bfs_persistent, kThreads, 0, o.blocks_per_sm, args, nullptr);
+}
+
+// As igk_bfs, the source read on the device from *d_src_key (see BfsArgs).
+int igk_bfs_keyed(IgExec* ex, const ig_csr* dg, const unsigned long long* d_src_key, int* d_dist) {
+  const int src = 0;
+  const size_t vb = (size_t)dg->nodes * sizeof(int);
+  void *qa, *qb, *hubs;
+  int rc;
+  if ((rc = ig_scratch_get(ex->scratch, IG_SLOT_Q0, vb, &qa))) return rc;
+  if ((rc = ig_scratch_get(ex->scratch, IG_SLOT_Q1, vb, &qb))) return rc;
+  if ((rc = ig_scratch_get(ex->scratch, IG_SLOT_Q2, vb, &hubs))) return rc;
+  void* bits;
+  if ((rc = ig_scratch_get(ex->scratch, IG_SLOT_V0, 3 * (((size_t)dg->nodes + 31) / 32) * 4, &bits))) return rc;
+  if ((rc = ig_exec_reset(ex))) return rc;
+  const IgOptions& o = ig_exec_options(ex);
+  BfsArgs a{dg->nindex, dg->nlist, dg->nodes, dg->edges, src, d_dist, (int*)qa, (int*)qb, (int*)hubs,
+            ex->d_ctl, ex->timeout_ns, o.hub_degree, o.bfs_alpha, o.bfs_beta, nullptr, 0,
+            o.bfs_bitmap ? (unsigned*)bits : nullptr, d_src_key};
   void* args[] = {&a};
   return ig_launch_coop(ex, (const void*)bfs_persistent, kThreads, 0, o.blocks_per_sm, args, nullptr);
 }
@@ -236,7 +261,7 @@ int igk_bfs_multi(IgExec* ex, const ig_csr* dg, const int* d_sources, int nsourc
   const IgOptions& o = ig_exec_options(ex);
   BfsArgs a{dg->nindex, dg->nlist, dg->nodes, dg->edges, 0, d_dist, (int*)qa, (int*)qb, (int*)hubs,
             ex->d_ctl, ex->timeout_ns, o.hub_degree, o.bfs_alpha, o.bfs_beta, d_sources, nsources,
-            o.bfs_bitmap ? (unsigned*)bits : nullptr};
+            o.bfs_bitmap ? (unsigned*)bits : nullptr, nullptr};
   void* args[] = {&a};
   return ig_launch_coop(ex, (const void*)bfs_persistent, kThreads, 0, o.blocks_per_sm, args, nullptr);
 }
@@ -254,7 +279,7 @@ int igk_bfs_launch_prealloc(IgExec* ex, const ig_csr* dg, int src, int* d_dist, 
   if (o.blocks_per_sm > 0) per_sm = std::min(per_sm, o.blocks_per_sm);
   if (per_sm < 1) return ig_fail(IG_ERR_CUDA, "persistent kernel cannot be resident (occupancy 0)");
   BfsArgs a{dg->nindex, dg->nlist, dg->nodes, dg->edges, src, d_dist, qa, qb, hubs,
-            ex->d_ctl, ex->timeout_ns, o.hub_degree, o.bfs_alpha, o.bfs_beta, nullptr, 0, nullptr};
+            ex->d_ctl, ex->timeout_ns, o.hub_degree, o.bfs_alpha, o.bfs_beta, nullptr, 0, nullptr, nullptr};
   void* args[] = {&a};
   rc = ig_cuda_check((int)cudaLaunchCooperativeKernel((const void*)bfs_persistent, dim3(per_sm * ex->sms),
                                                       dim3(kThreads), args, 0, ex->stream),

@@ -206,6 +206,42 @@ __global__ void cc_compress(int* parent, int n) {
   }
 }
 
+// BFS-seeded form.  The seed is the vertex of largest degree (ties: the
+// smaller id), packed as (degree << 32) | (0xffffffff - id) and reduced with
+// one 64-bit atomicMax per warp.
+__global__ void cc_seed(const int* __restrict__ nindex, int n, unsigned long long* key) {
+  unsigned long long best = 0;
+  for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < n; v += gridDim.x * blockDim.x) {
+    const unsigned long long d = (unsigned)(__ldg(&nindex[v + 1]) - __ldg(&nindex[v]));
+    const unsigned long long k = (d << 32) | (0xffffffffu - (unsigned)v);
+    best = k > best ? k : best;
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const unsigned long long t = __shfl_xor_sync(IG_FULL, best, o);
+    best = t > best ? t : best;
+  }
+  if ((threadIdx.x & 31) == 0) atomicMax(key, best);
+}
+
+// After a BFS from the seed wrote levels into `label`: the smallest reached
+// id (the seed's component's minimum) into *giant.
+__global__ void cc_reached_min(const int* label, int n, int* giant) {
+  int m = ig::kInf;
+  for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < n; v += gridDim.x * blockDim.x)
+    if (label[v] != ig::kInf) m = min(m, v);
+  m = __reduce_min_sync(IG_FULL, m);
+  if ((threadIdx.x & 31) == 0 && m != ig::kInf) atomicMin(giant, m);
+}
+
+// Reached vertices point at that minimum (one finished tree); the others
+// start as their own roots for the hooking of their edges.
+__global__ void cc_from_levels(int* label, int n, const int* giant) {
+  const int m = *giant;
+  for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < n; v += gridDim.x * blockDim.x)
+    label[v] = label[v] != ig::kInf ? m : v;
+}
+
 // Disjoint union of graphs: the global min-id label minus the graph's first
 // vertex is the graph's own min-id label.  One block per graph.
 __global__ void cc_localize(int* label, const int* __restrict__ graph_vptr, int graphs) {
@@ -227,11 +263,34 @@ int igk_cc(IgExec* ex, const ig_csr* dg, int* d_label, bool sample) {
   const int n = dg->nodes;
   void* hubs;
   int rc;
-  if ((rc = ig_scratch_get(ex->scratch, IG_SLOT_Q2, (size_t)n * sizeof(int), &hubs))) return rc;
-  if ((rc = ig_exec_reset(ex))) return rc;
   const IgOptions& o = ig_exec_options(ex);
   const int grid_v = std::min((n + kThreads - 1) / kThreads, ex->sms * 16);
   const int grid_w = std::max(1, std::min((n + kThreads - 1) / kThreads, ex->sms * 8));
+  if (sample && o.cc_bfs_seed) {
+    // The component of the largest-degree vertex (the giant one of a skewed
+    // graph) is labelled by a BFS from it with its smallest reached id; the
+    // other vertices link all their edges by union-find (they never touch
+    // that component), skipping the reached ones.
+    void* key;
+    if ((rc = ig_scratch_get(ex->scratch, IG_SLOT_V2, 64, &key))) return rc;
+    if ((rc = ig_cuda_check((int)cudaMemsetAsync(key, 0, 64, ex->stream), "memset"))) return rc;
+    cc_seed<<<grid_v, kThreads, 0, ex->stream>>>(dg->nindex, n, (unsigned long long*)key);
+    ig_count_launches(1);
+    if ((rc = igk_bfs_keyed(ex, dg, (const unsigned long long*)key, d_label))) return rc;  // resets the control block
+    if ((rc = ig_scratch_get(ex->scratch, IG_SLOT_Q2, (size_t)n * sizeof(int), &hubs))) return rc;
+    if ((rc = ig_cuda_check((int)cudaMemsetAsync(&ex->d_ctl->i32[1], 0x7f, sizeof(int), ex->stream), "memset")))
+      return rc;
+    cc_reached_min<<<grid_v, kThreads, 0, ex->stream>>>(d_label, n, &ex->d_ctl->i32[1]);
+    cc_from_levels<<<grid_v, kThreads, 0, ex->stream>>>(d_label, n, &ex->d_ctl->i32[1]);
+    cc_hook<<<grid_w, kThreads, 0, ex->stream>>>(dg->nindex, dg->nlist, n, d_label, (int*)hubs, ex->d_ctl,
+                                                 o.hub_degree, 0);
+    cc_hook_hubs<<<ex->sms * 4, kThreads, 0, ex->stream>>>(dg->nindex, dg->nlist, d_label, (int*)hubs, ex->d_ctl);
+    cc_compress<<<grid_v, kThreads, 0, ex->stream>>>(d_label, n);
+    ig_count_launches(5);
+    return ig_cuda_check((int)cudaGetLastError(), "cc launch");
+  }
+  if ((rc = ig_scratch_get(ex->scratch, IG_SLOT_Q2, (size_t)n * sizeof(int), &hubs))) return rc;
+  if ((rc = ig_exec_reset(ex))) return rc;
   cc_init<<<grid_v, kThreads, 0, ex->stream>>>(dg->nindex, dg->nlist, n, d_label);
   if (sample && o.cc_rounds == 2) {  // the init forest flattened before the sampled unions
     cc_compress<<<grid_v, kThreads, 0, ex->stream>>>(d_label, n);

@@ -366,18 +366,19 @@ def test_sssp_item_pass_forms(ig, orc, graphs, merge_below, spin):
             ig.set_option(k, v)
 
 
-@pytest.mark.parametrize("opt,values", [("bfs_bitmap", (0, 1)), ("cc_rounds", (0, 1))])
+@pytest.mark.parametrize("opt,values", [("bfs_bitmap", (0, 1)), ("cc_rounds", (0, 1, 2)), ("cc_bfs_seed", (0, 1))])
 def test_traversal_option_forms_match_oracle(ig, orc, graphs, opt, values):
-    """BFS with and without the level bitmaps of its bottom-up levels (forced
-    bottom-up from the first level too), CC with the sampled neighbours linked
-    in one pass or one round each: the results are exact every way."""
+    """BFS with and without the level bitmaps of its bottom-up levels (pulling
+    from the first level too), CC with the sampled neighbours linked in one
+    pass, one round each or after flattening, and CC whose largest-degree
+    component is labelled by a BFS: the results are exact every way."""
     old = {k: ig.get_option(k) for k in (opt, "bfs_alpha")}
     try:
         for val in values:
             ig.set_option(opt, val)
             for alpha in (14, 1):
                 ig.set_option("bfs_alpha", alpha)
-                for name in ("rmat14", "hubby", "road128", "two_grids", "star"):
+                for name in ("rmat14", "hubby", "road128", "two_grids", "star", "single", "two_isolated", "er4k"):
                     g = graphs[name]
                     r = run_all(ig, g, [0, g.nodes // 2])
                     for k, s in enumerate([0, g.nodes // 2]):
