@@ -31,7 +31,8 @@ struct IgOptions {
   int tc_grab;            // TC: block work items taken in runs of this many from a counter, so a middle
                           // vertex's items mostly share one block and its table (0: grid stride)
   int cc_bfs_seed;        // CC: 1 = the largest-degree vertex's component labelled by a BFS from it,
-                          // union-find for the rest (0 = neighbour sampling, then union-find)
+                          // union-find for the rest (0 = neighbour sampling, then union-find;
+                          // cc_rounds chooses the sampling form)
   int cc_rounds;          // CC: 1 = sampled neighbours linked one round at a time (read-only root
                           // searches, a compression after each), 0 = both in one pass with path
                           // halving, 2 = as 0 after flattening the initial forest

@@ -673,7 +673,7 @@ IgOptions& ig_options() {
       /*pr_two_pass=*/0,
       /*tc_block_chunk=*/4096,
       /*tc_grab=*/2,
-      /*cc_bfs_seed=*/0,
+      /*cc_bfs_seed=*/1,
       /*cc_rounds=*/0,
   };
   return o;

@@ -50,11 +50,12 @@ BIG = 1 << 30
 #        Dijkstra order, NoWindow; sync: Sync2 = work items after a second
 #        grid barrier per round, Sync1 = within the round (one barrier);
 #        Plain / LightHeavy edge split.  (Always a data-driven worklist.)
-#   CC   link: Pass = sampled neighbours linked in one pass with path
-#        halving, Rounds = one round per neighbour with a compression after
-#        each, FlatPass = Pass after flattening the initial forest, BfsSeed =
-#        the largest-degree vertex's component labelled by a BFS (data-driven
-#        traversal), union-find for the rest; granularity as BFS.  (Hooking pushes along edges.)
+#   CC   link: BfsSeed = the largest-degree vertex's component labelled by
+#        a BFS from it (direction-optimising traversal), union-find for the
+#        rest; Pass = neighbour sampling (two neighbours linked in one pass
+#        with path halving), Rounds = one round per sampled neighbour with a
+#        compression after each, FlatPass = Pass after flattening the initial
+#        forest; granularity as BFS.  (Hooking pushes along edges.)
 #   MIS  residency only (B4 / B2 / B8 blocks per SM).
 #   PR   gather: OnePass = contributions gathered while summing, TwoPass =
 #        every edge's contribution gathered first in one dense pass (measured
@@ -73,8 +74,8 @@ STYLES = {
              "order": {"Window": {}, "NoWindow": {"sssp_window_scale": 0}},
              "sync": {"Sync2": {}, "Sync1": {"sssp_merge_below": BIG}},
              "split": {"Plain": {}, "LightHeavy": {"sssp_heavy_split": 1}}},
-    "cc": {"link": {"Pass": {}, "Rounds": {"cc_rounds": 1}, "FlatPass": {"cc_rounds": 2},
-                    "BfsSeed": {"cc_bfs_seed": 1}},
+    "cc": {"link": {"BfsSeed": {}, "Pass": {"cc_bfs_seed": 0}, "Rounds": {"cc_bfs_seed": 0, "cc_rounds": 1},
+                    "FlatPass": {"cc_bfs_seed": 0, "cc_rounds": 2}},
            "granularity": {"WarpGrid": {}, "Grid": {"hub_degree": 64}, "Warp": {"hub_degree": BIG}}},
     "mis": {"residency": {"B4": {}, "B2": {"blocks_per_sm": 2}, "B8": {"blocks_per_sm": 8}}},
     "pr": {"gather": {"OnePass": {}, "TwoPass": {"pr_two_pass": 1}},
