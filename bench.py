@@ -491,11 +491,11 @@ def load_peaks() -> dict:
 # 21`: 63,539,260 edges), scaled to RMAT-22 by the edge ratio 2.019 (the
 # traffic grows with the edges processed).  Kernels: sssp_persistent,
 # pr_persistent (15 iterations), tc_count_block (exact and hashed forms; the
-# orientation kernels are not included), bfs_persistent, mis_persistent,
-# cc_sample (CC's largest kernel).  The capture and its figures are in the
-# per-kernel traffic summary under profiles/.
+# orientation kernels are not included), bfs_persistent, mis_persistent.
+# The capture and its figures are in the per-kernel traffic summary under
+# profiles/.
 DRAM_BYTES_PER_CALL = {"sssp": 2497888874, "pr": 9041198075, "tc": 4028693498, "bfs": 155368847,
-                       "mis": 167385116, "cc": 148094672}
+                       "mis": 167385116}
 
 
 # ----------------------------------------------------------------------------- CPU
