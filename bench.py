@@ -494,7 +494,7 @@ def load_peaks() -> dict:
 # orientation kernels are not included), bfs_persistent, mis_persistent.
 # The capture and its figures are in the per-kernel traffic summary under
 # profiles/.
-DRAM_BYTES_PER_CALL = {"sssp": 2497888874, "pr": 9041198075, "tc": 4028693498, "bfs": 155368847,
+DRAM_BYTES_PER_CALL = {"sssp": 2497888874, "pr": 9041198075, "tc": 3688275862, "bfs": 155368847,
                        "mis": 167385116}
 
 
