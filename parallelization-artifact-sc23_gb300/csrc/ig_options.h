@@ -20,6 +20,8 @@ struct IgOptions {
   int sssp_spin_ns;       // SSSP: pause between polls of a warp waiting for work items (merged rounds)
   int sssp_pair_slices;   // SSSP: work-item slices expanded two at a time (eight edges per lane):
                           // 1 = at 3 blocks per SM, 2 = at 4 (register spills); 0 = one at a time
+  int sssp_stage_flags;   // SSSP: 1 = improved vertices staged per warp in shared memory and their
+                          // queue flags settled 32 at a time; 0 = settled by the step that found them
   int pr_hub_degree;      // PageRank: degree above which a vertex is split in chunks
   int pr_chunk;           // PageRank: edges per hub chunk
   int pr_blocks_per_sm;   // PageRank: resident blocks per SM (0 = blocks_per_sm)

@@ -665,6 +665,7 @@ IgOptions& ig_options() {
       /*sssp_merge_below=*/0,
       /*sssp_spin_ns=*/1000,
       /*sssp_pair_slices=*/0,
+      /*sssp_stage_flags=*/1,
       /*pr_hub_degree=*/1024,
       /*pr_chunk=*/4096,
       /*pr_blocks_per_sm=*/4,
@@ -694,6 +695,7 @@ static const OptField g_opt_fields[] = {
     IG_OPT(sssp_heavy_split, 0, 1),   IG_OPT(sssp_item_edges, 32, 4096), IG_OPT(sssp_warp_degree, 1, INT_MAX),
     IG_OPT(sssp_window_scale, 0, 1 << 20), IG_OPT(sssp_window_degree, 0, INT_MAX),
     IG_OPT(sssp_merge_below, 0, INT_MAX),   IG_OPT(sssp_spin_ns, 0, 100000), IG_OPT(sssp_pair_slices, 0, 2),
+    IG_OPT(sssp_stage_flags, 0, 1),
     IG_OPT(pr_hub_degree, 32, INT_MAX), IG_OPT(pr_chunk, 32, 1 << 24),
     IG_OPT(pr_blocks_per_sm, 0, 32), IG_OPT(pr_prefetch, 0, 1), IG_OPT(pr_subwarp, 0, 1), IG_OPT(pr_two_pass, 0, 1), IG_OPT(tc_block_chunk, 256, 1 << 16), IG_OPT(tc_grab, 0, 64), IG_OPT(cc_bfs_seed, 0, 1), IG_OPT(cc_rounds, 0, 2),
 };

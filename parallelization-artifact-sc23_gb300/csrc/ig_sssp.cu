@@ -80,6 +80,7 @@ struct SsspArgs {
   int window_degree;     // vertices of at most this degree are never deferred
   int merge_below;       // rounds with a smaller frontier expand their items without a second barrier
   int spin_ns;           // pause between polls of a warp waiting for work items
+  int stage_flags;       // 1: improved vertices staged per warp, their queue flags settled 32 at a time
 };
 
 // Per-round counters: hot counters of the control block (every warp updates
@@ -123,9 +124,13 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) sssp_persistent(SsspArgs
   const int warp_g = (int)(gtid >> 5);
   const int nwarps = (int)(gthreads >> 5);
   __shared__ int s_qbuf[kThreads / 32][2][kPair ? kQBuf : kWarpBuf];  // per-warp staging of near / far appends
+  // per-warp staging of improved vertices (vertex, new distance) whose queue
+  // flags are not settled yet: fewer than 32 between steps, plus one step's
+  __shared__ int2 s_cand[kThreads / 32][kPair ? kQBuf : kWarpBuf];
   int* nbuf = s_qbuf[threadIdx.x >> 5][0];
   int* fbuf = s_qbuf[threadIdx.x >> 5][1];
-  int nbuf_n = 0, fbuf_n = 0;
+  int2* cbuf = s_cand[threadIdx.x >> 5];
+  int nbuf_n = 0, fbuf_n = 0, cbuf_n = 0;
 
   for (long long v = gtid; v < a.nodes; v += gthreads) {
     a.dist[v] = (v == a.src) ? 0 : kInf;
@@ -220,13 +225,46 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) sssp_persistent(SsspArgs
         const int nprev = min(ld_relaxed(ci(kCItems + (it + 2) % 3)), kSmallItems);
         for (long long i = gtid; i < nprev; i += gthreads) old_small[i] = kNoItem;
       }
-      // Four edges per lane at a time: their loads, atomics and stamp checks
-      // are independent, so they are issued together.  The distance update is
-      // a reduction (atomicMin without a result): an edge whose candidate beats
+      // Queue flags of one improved vertex per lane (lanes < cnt): a distance
+      // below T joins the next near queue once per iteration (stamp), any
+      // other the far pile once per epoch (flag).
+      auto settle = [&](int cnt, int v, int nd) {
+        bool tn = false, tf = false;
+        if (ig::lane_id() < cnt) {
+          if (nd < T) {
+            nmin = min(nmin, nd);
+            tn = a.stamp[v] != next_stamp && atomicExch(&a.stamp[v], next_stamp) != next_stamp;
+          } else {
+            tf = a.farflag[v] != far_mark && atomicExch(&a.farflag[v], far_mark) != far_mark;
+          }
+        }
+        const int vv[1] = {v};
+        const bool fn[1] = {tn}, ff[1] = {tf};
+        warp_buf_append2_flags<1>(vv, fn, nbuf, nbuf_n, nxt, qsize, ff, fbuf, fbuf_n, far, fsize, a.nodes, ctl);
+      };
+      // Settles staged improved vertices 32 at a time (all of them if `all`).
+      auto settle_staged = [&](bool all) {
+        __syncwarp();
+        while (cbuf_n >= 32 || (all && cbuf_n > 0)) {
+          const int take = min(cbuf_n, 32);
+          cbuf_n -= take;
+          int2 c = make_int2(0, 0);
+          if (lane < take) c = cbuf[cbuf_n + lane];
+          __syncwarp();
+          settle(take, c.x, c.y);
+        }
+      };
+      // Four edges per lane at a time: their loads and atomics are
+      // independent, so they are issued together.  The distance update is a
+      // reduction (atomicMin without a result): an edge whose candidate beats
       // the distance it read counts as an improvement without waiting for the
       // atomic.  Another edge may have lowered the distance further in the
       // meantime; the vertex is then queued once more than needed (the stamp
       // keeps it to one entry per queue, the expanded-distance check skips it).
+      // With stage_flags the improved vertices go to the warp's staging
+      // buffer and their flags are settled once 32 have gathered, so a step
+      // waits for two dependent reads (list, then distances) instead of four
+      // (and the flag exchanges); otherwise each step settles its own.
       auto relax4 = [&](const auto& act, const auto& e, const auto& du) {
         constexpr int N = std::extent<std::remove_reference_t<decltype(act)>>::value;  // 4, or 8 for two slices
         int v[N], w[N], dv[N], sv[N];
@@ -247,6 +285,19 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) sssp_persistent(SsspArgs
           const bool light = !a.heavy_split || (long long)w[k] < delta;
           cand[k] = act[k] && du[k] != kInf && light != heavy && (long long)du[k] + w[k] < (long long)dv[k];
           if (cand[k]) atomicMin(&a.dist[v[k]], du[k] + w[k]);
+        }
+        if (a.stage_flags) {
+#pragma unroll
+          for (int k = 0; k < N; k++) {
+            const unsigned m = __ballot_sync(IG_FULL, cand[k]);
+            if (cand[k]) {
+              improved++;
+              cbuf[cbuf_n + __popc(m & lanemask_lt())] = make_int2(v[k], du[k] + w[k]);
+            }
+            cbuf_n += __popc(m);
+          }
+          if (cbuf_n >= 32) settle_staged(false);
+          return;
         }
 #pragma unroll
         for (int k = 0; k < N; k++) sv[k] = cand[k] ? a.stamp[v[k]] : 0;
@@ -438,6 +489,7 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) sssp_persistent(SsspArgs
         }
       };
       auto end_pass = [&]() {
+        settle_staged(true);
         warp_buf_flush(nbuf, nbuf_n, nxt, qsize, a.nodes, ctl);
         warp_buf_flush(fbuf, fbuf_n, far, fsize, a.nodes, ctl);
         publish_min(nmin, ci(kCMin + (it + 1) % 3));
@@ -639,7 +691,7 @@ int igk_sssp(IgExec* ex, const ig_csr* dg, int src, int* d_dist) {
              (int*)expanded, (int*)members, (int*)inmember, ex->d_ctl, ex->timeout_ns, o.sssp_item_edges,
              o.sssp_warp_degree,
              o.sssp_delta, o.sssp_delta_scale, o.sssp_heavy_split, o.sssp_window_scale,
-             o.sssp_window_degree, o.sssp_merge_below, o.sssp_spin_ns};
+             o.sssp_window_degree, o.sssp_merge_below, o.sssp_spin_ns, o.sssp_stage_flags};
   void* args[] = {&a};
   // the register budget follows the residency cap (4, 5 or 6 blocks of 256 threads per SM)
   // (the paired-slice form holds more registers: 3 blocks per SM, or 4 with spills)

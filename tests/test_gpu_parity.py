@@ -447,6 +447,32 @@ def test_sssp_paired_slices(ig, orc, graphs, pair):
             ig.set_option(k, v)
 
 
+@pytest.mark.parametrize("stage,heavy,pair", [(0, 0, 0), (1, 0, 0), (1, 1, 0), (0, 1, 0), (1, 0, 1)])
+def test_sssp_flag_settling_forms(ig, orc, graphs, stage, heavy, pair):
+    """Improved vertices staged per warp and their queue flags settled 32 at
+    a time, or settled by the step that found them; with and without the
+    light/heavy edge split and the paired slices: exact distances, with most
+    lists cut into work items (threshold 4) and with the default threshold."""
+    old = {k: ig.get_option(k) for k in ("sssp_stage_flags", "sssp_heavy_split", "sssp_pair_slices",
+                                         "sssp_warp_degree")}
+    try:
+        ig.set_option("sssp_stage_flags", stage)
+        ig.set_option("sssp_heavy_split", heavy)
+        ig.set_option("sssp_pair_slices", pair)
+        for wd in (64, 4):
+            ig.set_option("sssp_warp_degree", wd)
+            for name in ("rmat14", "hubby", "road128", "star", "rmat18"):
+                g = graphs[name]
+                with ig.DeviceCSR(g) as d:
+                    for s in (0, g.nodes // 2):
+                        dist = np.empty(g.nodes, np.int32)
+                        ig.GPUsssp_vertex(int(s), d, dist)
+                        assert np.array_equal(dist, orc.sssp(g, int(s))), (name, s, wd)
+    finally:
+        for k, v in old.items():
+            ig.set_option(k, v)
+
+
 @pytest.mark.parametrize("grab", [1, 4, 16])
 def test_tc_item_runs(ig, orc, graphs, grab):
     """Block work items taken in runs from a counter instead of a grid
