@@ -60,6 +60,7 @@ __global__ void __launch_bounds__(kThreads) bfs_persistent(BfsArgs a_in) {
   BfsArgs a = a_in;
   using namespace ig;
   IgCtl* ctl = a.ctl;
+  GridBar gb;  // this block's view of the barrier generation
   const int lane = lane_id();
   const long long gtid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   const long long gthreads = (long long)gridDim.x * blockDim.x;
@@ -80,7 +81,7 @@ __global__ void __launch_bounds__(kThreads) bfs_persistent(BfsArgs a_in) {
   } else {
     // several sources (one per graph of a disjoint union): all start at level 0
     for (long long v = gtid; v < a.nodes; v += gthreads) a.dist[v] = kInf;
-    if (!grid_sync(ctl, a.timeout_ns)) return;
+    if (!grid_sync(ctl, a.timeout_ns, gb)) return;
     for (long long i = gtid; i < a.nsources; i += gthreads) {
       a.dist[a.sources[i]] = 0;
       a.qa[i] = a.sources[i];
@@ -89,7 +90,7 @@ __global__ void __launch_bounds__(kThreads) bfs_persistent(BfsArgs a_in) {
     cur_size = a.nsources;
     src_deg = a.edges / 2;  // start top-down; the switch rule takes over after level 0
   }
-  if (!grid_sync(ctl, a.timeout_ns)) return;
+  if (!grid_sync(ctl, a.timeout_ns, gb)) return;
 
   int* cur = a.qa;
   int* nxt = a.qb;
@@ -145,11 +146,11 @@ __global__ void __launch_bounds__(kThreads) bfs_persistent(BfsArgs a_in) {
         warp_append(hub, v, a.hubs, nhub, a.nodes, ctl);
         warp_expand(beg, hub ? 0 : deg, visit);
       }
-      if (!grid_sync(ctl, a.timeout_ns)) return;
+      if (!grid_sync(ctl, a.timeout_ns, gb)) return;
       const int nh = ld_relaxed(nhub);
       if (nh > 0) {
         grid_expand_hubs(a.nindex, a.hubs, nh, [&](bool act, int e, int) { visit(act, e, 0); });
-        if (!grid_sync(ctl, a.timeout_ns)) return;
+        if (!grid_sync(ctl, a.timeout_ns, gb)) return;
       }
     } else {
       for (long long base = gtid & ~31LL; base < a.nodes; base += gthreads) {
@@ -186,7 +187,7 @@ __global__ void __launch_bounds__(kThreads) bfs_persistent(BfsArgs a_in) {
         }
         warp_append_w(found, (int)v, deg, nxt, qsize, fedges, a.nodes, ctl);
       }
-      if (!grid_sync(ctl, a.timeout_ns)) return;
+      if (!grid_sync(ctl, a.timeout_ns, gb)) return;
     }
 
     const int nf = ld_relaxed(qsize);

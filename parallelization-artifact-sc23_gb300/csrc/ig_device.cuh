@@ -87,31 +87,58 @@ __device__ __forceinline__ unsigned long long* hot64(IgCtl* ctl, int k) {
   return (unsigned long long*)&ctl->hot[k * kCtlSpread];
 }
 
-// Records the first device-side error.
-__device__ __forceinline__ void raise(IgCtl* ctl, int code) { atomicCAS(&ctl->err, 0, code); }
+// Top bit of the grid barrier's arrival count: set by every raise, so the
+// last block to arrive learns of an error from its own arrival (see grid_sync).
+constexpr unsigned kArriveErr = 0x80000000u;
+
+// Records the first device-side error (and flags it to the grid barrier).
+__device__ __forceinline__ void raise(IgCtl* ctl, int code) {
+  atomicCAS(&ctl->err, 0, code);
+  atomicOr(&ctl->sync.arrive, kArriveErr);
+}
 
 // Grid-wide barrier for a cooperative launch.  Returns false (in every
-// thread of the block) when the barrier failed: another block raised an
-// error, or the wait exceeded `timeout_ns`; the caller must then return.
-// Pattern: block barrier, one thread publishes its block's writes with a
-// gpu-scope fence and arrives; the last arriver resets the count and bumps
-// the generation with release semantics; the others spin on an acquire load
-// of the generation (bounded), then fence and release their block.
-__device__ __forceinline__ bool grid_sync(IgCtl* ctl, unsigned long long timeout_ns) {
+// thread of the block) when the barrier failed: a block raised an error
+// before arriving, or the wait exceeded `timeout_ns`; the caller must then
+// return.  Pattern: block barrier, one thread publishes its block's writes
+// with a gpu-scope fence and arrives; the last arriver resets the count and
+// bumps the generation with release semantics, its top bit set when the
+// arrival count carried the error flag (every raise flags it, so a raise
+// before any block's arrival is seen by the last arriver's own atomic); the
+// others spin on an acquire load of the generation (bounded, watching the
+// error word), then fence and release their block.
+// `GridBar` keeps the block's view of the generation between barriers, so a
+// barrier costs one atomic round trip and the wait (the generation is read
+// once per kernel, at its first barrier; blocks cannot pass a barrier before
+// every block has arrived, so all read the same value).
+constexpr unsigned kGenErr = 0x80000000u;
+struct GridBar {
+  unsigned gen = 0;
+  bool known = false;
+};
+
+__device__ __forceinline__ bool grid_sync(IgCtl* ctl, unsigned long long timeout_ns, GridBar& gb) {
   __shared__ int s_ok;
   __syncthreads();
   if (threadIdx.x == 0) {
     int ok = 1;
     IgSync* s = &ctl->sync;
-    const unsigned gen = ld_acquire(&s->gen);
+    if (!gb.known) {
+      gb.gen = ld_acquire(&s->gen) & ~kGenErr;
+      gb.known = true;
+    }
+    const unsigned next = (gb.gen + 1) & ~kGenErr;
     __threadfence();
-    if (atom_add_acqrel(&s->arrive, 1u) == gridDim.x - 1) {
+    const unsigned old = atom_add_acqrel(&s->arrive, 1u);
+    if ((old & ~kArriveErr) == gridDim.x - 1) {
       atomicExch(&s->arrive, 0u);
-      st_release(&s->gen, gen + 1);
+      const unsigned e = (old & kArriveErr) ? kGenErr : 0u;
+      st_release(&s->gen, next | e);
+      ok = e == 0;
     } else {
       const unsigned long long t0 = globaltimer();
-      unsigned spins = 0;
-      while (ld_acquire(&s->gen) == gen) {
+      unsigned spins = 0, g;
+      while (((g = ld_acquire(&s->gen)) & ~kGenErr) == gb.gen) {
         if ((++spins & 63u) == 0) {
           if (ld_relaxed(&ctl->err) != 0) { ok = 0; break; }
           if (globaltimer() - t0 > timeout_ns) {
@@ -122,13 +149,21 @@ __device__ __forceinline__ bool grid_sync(IgCtl* ctl, unsigned long long timeout
         }
         __nanosleep(32);
       }
+      if (ok && (g & kGenErr)) ok = 0;
     }
+    gb.gen = next;
     __threadfence();
-    if (ld_relaxed(&ctl->err) != 0) ok = 0;
     s_ok = ok;
   }
   __syncthreads();
   return s_ok != 0;
+}
+
+// The same barrier for a kernel that keeps no GridBar (the generation is
+// read at every call).
+__device__ __forceinline__ bool grid_sync(IgCtl* ctl, unsigned long long timeout_ns) {
+  GridBar gb;
+  return grid_sync(ctl, timeout_ns, gb);
 }
 
 // Warp-aggregated append: every lane of a converged warp calls it; lanes with
@@ -531,6 +566,28 @@ __device__ __forceinline__ void warp_buf_append2_flags(const int (&v)[kMax], con
   __syncwarp();
   warp_buf_drain(b1, n1, q1, s1, cap, ctl);
   warp_buf_drain(b2, n2, q2, s2, cap, ctl);
+}
+
+// warp_buf_flush of two buffers (fewer than 32 items each) with both queue
+// reservations in flight together.
+__device__ __forceinline__ void warp_buf_flush2(int* b1, int& n1, int* q1, int* s1, int* b2, int& n2, int* q2,
+                                                int* s2, int cap, IgCtl* ctl) {
+  if ((n1 | n2) == 0) return;  // warp-uniform
+  const int lane = lane_id();
+  int base = 0;
+  if (lane == 0 && n1) base = atomicAdd(s1, n1);
+  if (lane == 1 && n2) base = atomicAdd(s2, n2);
+  const int p1 = __shfl_sync(IG_FULL, base, 0), p2 = __shfl_sync(IG_FULL, base, 1);
+  if (lane < n1) {
+    if (p1 + lane < cap) q1[p1 + lane] = b1[lane];
+    else raise(ctl, IG_ERR_OVERFLOW);
+  }
+  if (lane < n2) {
+    if (p2 + lane < cap) q2[p2 + lane] = b2[lane];
+    else raise(ctl, IG_ERR_OVERFLOW);
+  }
+  __syncwarp();
+  n1 = n2 = 0;
 }
 
 __device__ __forceinline__ void warp_buf_flush(int* buf, int& n, int* q, int* qsize, int cap, IgCtl* ctl) {

@@ -58,6 +58,7 @@ __device__ __forceinline__ bool larger(unsigned pn, int n, unsigned pv, int v) {
 __global__ void __launch_bounds__(kThreads) mis_persistent(MisArgs a) {
   using namespace ig;
   IgCtl* ctl = a.ctl;
+  GridBar gb;  // this block's view of the barrier generation
   const int lane = lane_id();
   const long long gtid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   const long long gthreads = (long long)gridDim.x * blockDim.x;
@@ -67,7 +68,7 @@ __global__ void __launch_bounds__(kThreads) mis_persistent(MisArgs a) {
     a.status[v] = kUndecided;
     a.resume[v] = __ldg(&a.nindex[v]);
   }
-  if (!grid_sync(ctl, a.timeout_ns)) return;
+  if (!grid_sync(ctl, a.timeout_ns, gb)) return;
 
   int* cur = a.wa;
   int* nxt = a.wb;
@@ -162,7 +163,7 @@ __global__ void __launch_bounds__(kThreads) mis_persistent(MisArgs a) {
       if (lane == 0) nb = nwarps * 32 * gch + atomicAdd(grab, 32 * gch);
       base0 = __shfl_sync(IG_FULL, nb, 0);
     }
-    if (!grid_sync(ctl, a.timeout_ns)) return;
+    if (!grid_sync(ctl, a.timeout_ns, gb)) return;
     cur_size = ld_relaxed(wsize);
     round++;
     int* t = cur;

@@ -240,6 +240,7 @@ __global__ void __launch_bounds__(kThreads, 4) pr_persistent(PrArgs a) {
   __shared__ int s_scan[33];
   __shared__ double s_red[32];
   IgCtl* ctl = a.ctl;
+  GridBar gb;  // this block's view of the barrier generation
   const int lane = lane_id();
   const int G = gridDim.x;
   const long long gtid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -272,7 +273,7 @@ __global__ void __launch_bounds__(kThreads, 4) pr_persistent(PrArgs a) {
       a.blk[G + blockIdx.x] = tc;
     }
   }
-  if (!grid_sync(ctl, a.timeout_ns)) return;
+  if (!grid_sync(ctl, a.timeout_ns, gb)) return;
   // ---- deterministic compaction of the hubs (in vertex order)
   {
     int hoff = 0, coff = 0, htot = 0, ctot = 0;
@@ -307,13 +308,13 @@ __global__ void __launch_bounds__(kThreads, 4) pr_persistent(PrArgs a) {
       a.chunk_base[htot] = ctot;
     }
   }
-  if (!grid_sync(ctl, a.timeout_ns)) return;
+  if (!grid_sync(ctl, a.timeout_ns, gb)) return;
   const int nh = ld_relaxed(&ctl->i32[10]);
   const int nchunks = ld_relaxed(&ctl->i32[11]);
   // chunk -> hub map, so a chunk finds its hub with one load every iteration
   for (int h = warp_g; h < nh; h += nwarps)
     for (int c = a.chunk_base[h] + lane; c < a.chunk_base[h + 1]; c += 32) a.chunk_hub[c] = h;
-  if (!grid_sync(ctl, a.timeout_ns)) return;
+  if (!grid_sync(ctl, a.timeout_ns, gb)) return;
 
   float* cur = a.ca;
   float* nxt = a.cb;
@@ -356,7 +357,7 @@ __global__ void __launch_bounds__(kThreads, 4) pr_persistent(PrArgs a) {
         }
       }
       for (long long k = (nq << 2) + gtid; k < a.edges; k += gthreads) a.vals[k] = cur[__ldg(&a.nlist[k])];
-      if (!grid_sync(ctl, a.timeout_ns)) return;
+      if (!grid_sync(ctl, a.timeout_ns, gb)) return;
     }
     // ---- phase A: hub chunks (partial sums) and regular vertices
     for (int c = warp_g; c < nchunks; c += nwarps) {
@@ -476,7 +477,7 @@ __global__ void __launch_bounds__(kThreads, 4) pr_persistent(PrArgs a) {
     }
     // ---- phase B: combine hub chunks in chunk order
     if (nh > 0) {
-      if (!grid_sync(ctl, a.timeout_ns)) return;
+      if (!grid_sync(ctl, a.timeout_ns, gb)) return;
       for (int h = warp_g; h < nh; h += nwarps) {
         const int c0 = a.chunk_base[h], c1 = a.chunk_base[h + 1];
         float hi = 0.f, lo = 0.f;
@@ -509,7 +510,7 @@ __global__ void __launch_bounds__(kThreads, 4) pr_persistent(PrArgs a) {
     const double berr = block_sum_double(err, s_red);
     double* slot = a.blkerr + (it & 1) * G;
     if (threadIdx.x == 0) slot[blockIdx.x] = berr;
-    if (!grid_sync(ctl, a.timeout_ns)) return;
+    if (!grid_sync(ctl, a.timeout_ns, gb)) return;
     // the grid's residual: warp 0 of every block sums the block partials with
     // the same fixed tree (lane-strided sums, then a shuffle tree), so every
     // block reaches the same value and the same stop decision

@@ -39,6 +39,7 @@ namespace {
 
 constexpr int kThreads = 256;
 constexpr int kDeltaSamples = 4096;
+static_assert(kDeltaSamples % 32 == 0, "delta samples are taken by whole warps");
 constexpr int kSlice = 128;  // edges of a work-item slice: four per lane of one warp
 constexpr int kQBuf = 32 + 32 * 8;  // warp staging: 32 + the most one step adds (two slices, 8 per lane)
 static_assert(kSlice == 4 * 32, "a slice is one relax4 step of a warp");
@@ -81,6 +82,8 @@ struct SsspArgs {
   int merge_below;       // rounds with a smaller frontier expand their items without a second barrier
   int spin_ns;           // pause between polls of a warp waiting for work items
   int stage_flags;       // 1: improved vertices staged per warp, their queue flags settled 32 at a time
+  int chunk;             // frontier entries per warp chunk (at most 32)
+  int item_group;        // most work-item slices a warp takes at a time
 };
 
 // Per-round counters: hot counters of the control block (every warp updates
@@ -116,6 +119,7 @@ template <int kMinBlocks, bool kPair>
 __global__ void __launch_bounds__(kThreads, kMinBlocks) sssp_persistent(SsspArgs a) {
   using namespace ig;
   IgCtl* ctl = a.ctl;
+  GridBar gb;  // this block's view of the barrier generation
   auto ci = [&](int k) { return hot32(ctl, k); };
   auto cu = [&](int k) { return hot64(ctl, k); };
   const int lane = lane_id();
@@ -139,10 +143,15 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) sssp_persistent(SsspArgs
     a.expanded[v] = kInf;
     if (a.heavy_split) a.inmember[v] = 0;  // read only by the light/heavy split
   }
-  if (gtid < kDeltaSamples && a.edges > 0) {
+  if (gtid < kDeltaSamples && a.edges > 0) {  // whole warps (kDeltaSamples is a multiple of 32)
     const long long e = gtid * a.edges / kDeltaSamples;
-    atomicAdd(&ctl->u64[0], (unsigned long long)max(0, __ldg(&a.eweight[e])));
-    atomicAdd(&ctl->u64[1], 1ull);
+    unsigned long long w = (unsigned long long)max(0, __ldg(&a.eweight[e]));
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) w += __shfl_xor_sync(IG_FULL, w, o);
+    if (lane == 0) {
+      atomicAdd(&ctl->u64[0], w);
+      atomicAdd(&ctl->u64[1], 32ull);
+    }
   }
   for (long long i = gtid; i < kSmallItems; i += gthreads) {
     a.small0[i] = kNoItem;
@@ -155,7 +164,7 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) sssp_persistent(SsspArgs
       *cu(k) = (k >= kCFarMin && k < kCDone) ? ~0ull : 0ull;
     else *ci(k) = (k >= kCMin && k < kCMin + 3) ? kInf : 0;
   }
-  if (!grid_sync(ctl, a.timeout_ns)) return;
+  if (!grid_sync(ctl, a.timeout_ns, gb)) return;
 
   const unsigned long long wcnt = ld_relaxed(&ctl->u64[1]);
   const double mean_w = wcnt ? (double)ld_relaxed(&ctl->u64[0]) / (double)wcnt : 1.0;
@@ -324,7 +333,7 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) sssp_persistent(SsspArgs
       // queue entries, fewer when the queue has less than 32 per warp, so a
       // small round's lists are spread over the whole grid.
       int* grab = ci(kCGrab + it % 3);
-      const int cs = fcount >= nwarps * 32 ? 32 : max(1, (fcount + nwarps - 1) / nwarps);
+      const int cs = fcount >= nwarps * a.chunk ? a.chunk : max(1, (fcount + nwarps - 1) / nwarps);
       for (int base = warp_g * cs; base < fcount;) {
         const int i = base + lane;
         int u = 0, beg = 0, deg = 0, du = kInf;
@@ -351,8 +360,12 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) sssp_persistent(SsspArgs
               if (wc > 0 && deg > a.window_degree && (long long)(du - mq) * deg >= wc) {
                 expand = false;
                 deg = 0;
-                nmin = min(nmin, du);
-                defer = a.stamp[u] != next_stamp && atomicExch(&a.stamp[u], next_stamp) != next_stamp;
+                if (a.stage_flags) {
+                  defer = true;  // staged below with its distance (below T: it is in the near queue)
+                } else {
+                  nmin = min(nmin, du);
+                  defer = a.stamp[u] != next_stamp && atomicExch(&a.stamp[u], next_stamp) != next_stamp;
+                }
               } else {
                 a.expanded[u] = du;
               }
@@ -360,7 +373,16 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) sssp_persistent(SsspArgs
 
           }
         }
-        {
+        if (a.stage_flags) {
+          // a deferred vertex is queued again through the staged settling
+          // (stamp, smallest queued distance), off this chunk's critical path
+          const unsigned m = __ballot_sync(IG_FULL, defer);
+          if (m) {
+            if (defer) cbuf[cbuf_n + __popc(m & lanemask_lt())] = make_int2(u, du);
+            cbuf_n += __popc(m);
+            if (cbuf_n >= 32) settle_staged(false);
+          }
+        } else {
           const int dq[1] = {u};
           warp_buf_append<1>(defer ? 1 : 0, dq, nbuf, nbuf_n, nxt, qsize, a.nodes, ctl);
         }
@@ -467,7 +489,7 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) sssp_persistent(SsspArgs
       // the 64-bit counter `cnt`.
       auto barrier_items = [&](const unsigned long long* list, int nm, unsigned long long* cnt) {
         const long long units = (long long)nm << slog;
-        const int g = (int)min(8LL, max(1LL, units / (4LL * nwarps)));
+        const int g = (int)min((long long)a.item_group, max(1LL, units / (4LL * nwarps)));
         for (long long j0 = (long long)warp_g * g; j0 < units;) {
           const long long j1 = min(j0 + g, units);
           const int mfirst = (int)(j0 >> slog);
@@ -490,10 +512,9 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) sssp_persistent(SsspArgs
       };
       auto end_pass = [&]() {
         settle_staged(true);
-        warp_buf_flush(nbuf, nbuf_n, nxt, qsize, a.nodes, ctl);
-        warp_buf_flush(fbuf, fbuf_n, far, fsize, a.nodes, ctl);
+        warp_buf_flush2(nbuf, nbuf_n, nxt, qsize, fbuf, fbuf_n, far, fsize, a.nodes, ctl);
         publish_min(nmin, ci(kCMin + (it + 1) % 3));
-        return grid_sync(ctl, a.timeout_ns);
+        return grid_sync(ctl, a.timeout_ns, gb);
       };
       const int* icount = ci(kCItems + it % 3);
       bool end_barrier;  // the item pass needs a barrier of its own
@@ -615,7 +636,7 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) sssp_persistent(SsspArgs
         const int d = a.dist[far[i]];
         if ((long long)d >= T) atomicMin(cu(kCFarMin + f), (unsigned long long)d);
       }
-      if (!grid_sync(ctl, a.timeout_ns)) return;
+      if (!grid_sync(ctl, a.timeout_ns, gb)) return;
       const unsigned long long mfar = ld_relaxed(cu(kCFarMin + f));
       const long long T_old = T;
       if (mfar != ~0ull) T = ((long long)mfar > T ? (long long)mfar : T) + delta;
@@ -642,7 +663,7 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) sssp_persistent(SsspArgs
         warp_append(to_near, v, cur, qsize, a.nodes, ctl);
         warp_append(to_far, v, far_next, fsize_next, a.nodes, ctl);
       }
-      if (!grid_sync(ctl, a.timeout_ns)) return;
+      if (!grid_sync(ctl, a.timeout_ns, gb)) return;
       epoch++;
       cur_size = ld_relaxed(qsize);
     }
@@ -691,7 +712,7 @@ int igk_sssp(IgExec* ex, const ig_csr* dg, int src, int* d_dist) {
              (int*)expanded, (int*)members, (int*)inmember, ex->d_ctl, ex->timeout_ns, o.sssp_item_edges,
              o.sssp_warp_degree,
              o.sssp_delta, o.sssp_delta_scale, o.sssp_heavy_split, o.sssp_window_scale,
-             o.sssp_window_degree, o.sssp_merge_below, o.sssp_spin_ns, o.sssp_stage_flags};
+             o.sssp_window_degree, o.sssp_merge_below, o.sssp_spin_ns, o.sssp_stage_flags, o.sssp_chunk, o.sssp_item_group};
   void* args[] = {&a};
   // the register budget follows the residency cap (4, 5 or 6 blocks of 256 threads per SM)
   // (the paired-slice form holds more registers: 3 blocks per SM, or 4 with spills)
