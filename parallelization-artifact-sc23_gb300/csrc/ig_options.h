@@ -22,6 +22,8 @@ struct IgOptions {
                           // 1 = at 3 blocks per SM, 2 = at 4 (register spills); 0 = one at a time
   int sssp_stage_flags;   // SSSP: 1 = improved vertices staged per warp in shared memory and their
                           // queue flags settled 32 at a time; 0 = settled by the step that found them
+  int sssp_chunk;         // SSSP: frontier entries per warp chunk (1..32)
+  int sssp_item_group;    // SSSP: most work-item slices a warp claims at a time (1..32)
   int pr_hub_degree;      // PageRank: degree above which a vertex is split in chunks
   int pr_chunk;           // PageRank: edges per hub chunk
   int pr_blocks_per_sm;   // PageRank: resident blocks per SM (0 = blocks_per_sm)
@@ -32,6 +34,8 @@ struct IgOptions {
   int tc_block_chunk;     // TC: in-neighbours per block work item
   int tc_grab;            // TC: block work items taken in runs of this many from a counter, so a middle
                           // vertex's items mostly share one block and its table (0: grid stride)
+  int tc_warp_list;       // TC: probe lists at least this long are walked by the whole warp, shorter ones
+                          // share the warp's slots through an owner search
   int cc_bfs_seed;        // CC: 1 = the largest-degree vertex's component labelled by a BFS from it,
                           // union-find for the rest (0 = neighbour sampling, then union-find;
                           // cc_rounds chooses the sampling form)

@@ -41,22 +41,29 @@ constexpr int kThreads = 256;
 constexpr int kWarps = kThreads / 32;
 constexpr int kOrientHub = 256;   // lists longer than this are split by one block each
 constexpr int kBlockOut = 64;     // middle vertices with more out-neighbours are counted by whole blocks
+constexpr int kWarpOut = 128;     // ... unless no exact bitmap applies and they have at most this many
 constexpr int kChunk = 64;        // in-neighbours per warp work item
 constexpr int kHashCap = 2048;    // block table slots (out-degree <= 1024 is hashed)
 constexpr int kBitWords = 256;    // block filter: 8192 bits, bit (w mod 8192) set for w in N+(v)
-constexpr int kWarpCap = 128;     // warp table slots (out-degree <= kBlockOut)
+constexpr int kWarpCap = 256;     // warp table slots (out-degree <= kWarpOut)
 constexpr int kWarpBitWords = 64; // warp filter: 2048 bits
-constexpr int kWarpList = 96;     // in-neighbour lists this long are walked by the whole warp
 constexpr int kSpanWords = 4096;  // block bitmap: 131072 bits, bit (w - v - 1) set for w in N+(v)
 static_assert(kSpanWords >= kHashCap + kBitWords, "the bitmap shares its memory with the table and filter");
 
 // Work items of middle vertex v with `out` out-neighbours and `in`
 // in-neighbours: warp items of kChunk in-neighbours for a short N+(v), block
 // items of `block_chunk` for a long one (the block shares one table of N+(v)).
-__device__ __forceinline__ void tc_items(int out, int in, int block_chunk, int* warp_items, int* block_items) {
-  *warp_items = (out > 0 && out <= kBlockOut) ? (in + kChunk - 1) / kChunk : 0;
-  *block_items = out > kBlockOut ? (in + block_chunk - 1) / block_chunk : 0;
+// `exact`: N+(v) fits the block's exact bitmap (ids in (degree, id) order,
+// fewer than kSpanWords * 32 ids above v); without it a list of up to
+// kWarpOut stays with a warp (its own hash table, no block barrier per item:
+// such vertices have few in-neighbours in the skewed graphs this serves).
+__device__ __forceinline__ void tc_items(int out, int in, bool exact, int block_chunk, int* warp_items,
+                                         int* block_items) {
+  const bool block = out > kBlockOut && (exact || out > kWarpOut);
+  *warp_items = (out > 0 && !block) ? (in + kChunk - 1) / kChunk : 0;
+  *block_items = block ? (in + block_chunk - 1) / block_chunk : 0;
 }
+__device__ __forceinline__ bool tc_exact(bool ranked, int n, int v) { return ranked && n - 1 - v <= kSpanWords * 32; }
 
 __device__ __forceinline__ bool before(int du, int u, int dw, int w) { return du < dw || (du == dw && u < w); }
 
@@ -109,7 +116,7 @@ __global__ void __launch_bounds__(kThreads) tc_orient_count(const int* __restric
     if (v < n && !hub) {
       const int oc = s_cnt[wib][lane];
       out_cnt[v] = oc;
-      tc_items(oc, deg - oc, block_chunk, &item_cnt[v], &item_cnt_b[v]);
+      tc_items(oc, deg - oc, tc_exact(ranked, n, vv), block_chunk, &item_cnt[v], &item_cnt_b[v]);
     }
     __syncwarp();
   }
@@ -215,7 +222,7 @@ __global__ void __launch_bounds__(kThreads) tc_orient_hubs_count(const int* __re
     block_scan_int(keep, s_tmp, &total);
     if (threadIdx.x == 0) {
       out_cnt[u] = total;
-      tc_items(total, du - total, block_chunk, &item_cnt[u], &item_cnt_b[u]);
+      tc_items(total, du - total, tc_exact(ranked, n, u), block_chunk, &item_cnt[u], &item_cnt_b[u]);
     }
     __syncthreads();
   }
@@ -298,10 +305,11 @@ __device__ __forceinline__ unsigned long long probe_group(const int* __restrict_
                                                           const int* __restrict__ out_list,
                                                           const int* __restrict__ in_list, int g, int gend, int v,
                                                           int vb, int vd, bool ranked, const int* tab,
-                                                          const unsigned* bits, unsigned mask, bool hashed) {
+                                                          const unsigned* bits, unsigned mask, bool hashed,
+                                                          int warp_list) {
   using namespace ig;
   const int lane = lane_id();
-  unsigned long long local = 0;
+  unsigned hits = 0;  // this lane's, within one group
   int ub = 0, ud = 0;
   if (g + lane < gend) {
     const int u = __ldg(&in_list[g + lane]);
@@ -338,14 +346,16 @@ __device__ __forceinline__ unsigned long long probe_group(const int* __restrict_
     }
     return contains(out_list + vb, vd, w) ? 1 : 0;
   };
-  // long lists: the whole warp walks one list at a time, 128 probes per step,
-  // with no per-slot owner search
-  unsigned longs = __ballot_sync(IG_FULL, ud >= kWarpList);
+  // lists of at least warp_list probes: the whole warp walks one list at a
+  // time (no per-slot owner search), 128 probes per step while more than 96
+  // remain, then one step of 64 and one of 32 for the rest
+  unsigned longs = __ballot_sync(IG_FULL, ud >= warp_list);
   while (longs) {
     const int l = __ffs(longs) - 1;
     longs &= longs - 1;
     const int lb = __shfl_sync(IG_FULL, ub, l), le = lb + __shfl_sync(IG_FULL, ud, l);
-    for (int base = lb; base < le; base += 128) {
+    int base = lb;
+    for (; le - base > 96; base += 128) {
       int w[4];
 #pragma unroll
       for (int k = 0; k < 4; k++) {
@@ -354,10 +364,23 @@ __device__ __forceinline__ unsigned long long probe_group(const int* __restrict_
       }
 #pragma unroll
       for (int k = 0; k < 4; k++)
-        if (w[k] >= 0) local += probe(w[k]);
+        if (w[k] >= 0) hits += probe(w[k]);
     }
+    if (le - base > 32) {
+      int w[2];
+#pragma unroll
+      for (int k = 0; k < 2; k++) {
+        const int e = base + k * 32 + lane;
+        w[k] = e < le ? __ldg(&out_list[e]) : -1;
+      }
+#pragma unroll
+      for (int k = 0; k < 2; k++)
+        if (w[k] >= 0) hits += probe(w[k]);
+      base += 64;
+    }
+    if (base + lane < le) hits += probe(__ldg(&out_list[base + lane]));
   }
-  if (ud >= kWarpList) ud = 0;
+  if (ud >= warp_list) ud = 0;
   // short lists: four 32-probe slots per step, load-balanced over the lanes
   warp_expand4(ub, ud, [&](const bool (&act)[4], const int (&e)[4], const int (&)[4]) {
     int w[4];
@@ -365,9 +388,9 @@ __device__ __forceinline__ unsigned long long probe_group(const int* __restrict_
     for (int k = 0; k < 4; k++) w[k] = act[k] ? __ldg(&out_list[e[k]]) : -1;
 #pragma unroll
     for (int k = 0; k < 4; k++)
-      if (act[k]) local += probe(w[k]);
+      if (act[k]) hits += probe(w[k]);
   });
-  return local;
+  return hits;
 }
 
 // graph of vertex v in a batch: largest g with graph_vptr[g] <= v
@@ -389,7 +412,7 @@ __device__ __forceinline__ void tc_add_graph(unsigned long long mine, unsigned l
   if (ig::lane_id() == 0 && mine) atomicAdd(&count[tc_graph_of(graph_vptr, graphs, v)], mine);
 }
 
-// Warp work items: (middle vertex v with out-degree <= kBlockOut, kChunk of
+// Warp work items: (middle vertex v with out-degree <= kBlockOut, or <= kWarpOut without an exact bitmap, kChunk of
 // its in-neighbours).  The warp hashes N+(v) into its own small table.
 // kBatched: the graph is a disjoint union; triangles are added to the count of
 // the graph that holds their middle vertex (graph_vptr: first vertex of each graph).
@@ -401,7 +424,8 @@ __global__ void __launch_bounds__(kThreads) tc_count_warp(const int* __restrict_
                                                           const int* __restrict__ item_off,
                                                           const int* __restrict__ item_v, int n,
                                                           unsigned long long* count, const IgCtl* ctl,
-                                                          const int* __restrict__ graph_vptr, int graphs) {
+                                                          const int* __restrict__ graph_vptr, int graphs,
+                                                          int warp_list) {
   using namespace ig;
   __shared__ int s_tab[kWarps][kWarpCap + kWarpBitWords];
   if (ctl->err) return;
@@ -447,7 +471,7 @@ __global__ void __launch_bounds__(kThreads) tc_count_warp(const int* __restrict_
     const unsigned long long before_item = local;
     for (int g = c0; g < c1; g += 32)
       local += probe_group<kWarpBitWords>(out_off, out_list, in_list, g, c1, v, vb, vd, ranked, tab, bits, mask,
-                                          hashed);
+                                          hashed, warp_list);
     if (kBatched) tc_add_graph(local - before_item, count, graph_vptr, graphs, v);
   }
   if constexpr (!kBatched) {
@@ -473,7 +497,8 @@ __global__ void __launch_bounds__(kThreads, 8) tc_count_block(const int* __restr
                                                               const int* __restrict__ item_v, int n,
                                                               unsigned long long* count, const IgCtl* ctl,
                                                               const int* __restrict__ graph_vptr, int graphs,
-                                                              int block_chunk, int grab, int* grab_ctr) {
+                                                              int block_chunk, int grab, int* grab_ctr,
+                                                              int warp_list) {
   using namespace ig;
   // the exact bitmap, or the hash table followed by the filter
   __shared__ unsigned s_mem[kExact ? kSpanWords : kHashCap + kBitWords];
@@ -540,17 +565,22 @@ __global__ void __launch_bounds__(kThreads, 8) tc_count_block(const int* __restr
     const int c0 = ib + (it - __ldg(&item_off[v])) * block_chunk;
     const int c1 = min(c0 + block_chunk, iend);
     const unsigned long long before_item = local;
+    // groups of up to 32 in-neighbours per warp; an item with few takes
+    // smaller groups (at least 4), about two per warp, so they spread over
+    // the block's warps instead of leaving most of them at the next barrier
+    const int gsz = min(32, max(4, (c1 - c0 + 2 * kWarps - 1) / (2 * kWarps)));
     while (true) {
       int g = 0;
-      if (lane == 0) g = atomicAdd(&s_next, 32);
+      if (lane == 0) g = atomicAdd(&s_next, gsz);
       g = c0 + __shfl_sync(IG_FULL, g, 0);
       if (g >= c1) break;
+      const int ge = min(g + gsz, c1);
       if constexpr (kExact)
-        local += probe_group<kBitWords, true>(out_off, out_list, in_list, g, c1, v, vb, vd, true, tab, s_mem, mask,
-                                              false);
+        local += probe_group<kBitWords, true>(out_off, out_list, in_list, g, ge, v, vb, vd, true, tab, s_mem, mask,
+                                              false, warp_list);
       else
-        local += probe_group<kBitWords>(out_off, out_list, in_list, g, c1, v, vb, vd, ranked, tab, bits, mask,
-                                        hashed);
+        local += probe_group<kBitWords>(out_off, out_list, in_list, g, ge, v, vb, vd, ranked, tab, bits, mask,
+                                        hashed, warp_list);
     }
     if (kBatched) tc_add_graph(local - before_item, count, graph_vptr, graphs, v);
   }
@@ -580,6 +610,7 @@ static int tc_run(IgExec* ex, int nodes, int edges, const int* d_nindex, const i
   const size_t vb = ((size_t)nodes + 1) * sizeof(int);
   const int block_chunk = ig_exec_options(ex).tc_block_chunk;
   const int grab = ig_exec_options(ex).tc_grab;
+  const int wl = ig_exec_options(ex).tc_warp_list;
   void *cnt, *off, *icnt, *ioff, *icnt_b, *ioff_b, *list, *inl, *hubs, *itemv, *itemv_b;
   int rc;
   if ((rc = ig_scratch_get(ex->scratch, IG_SLOT_V0, vb, &cnt))) return rc;
@@ -625,23 +656,23 @@ static int tc_run(IgExec* ex, int nodes, int edges, const int* d_nindex, const i
   if (d_graph_vptr) {
     tc_count_block<true, true><<<cgrid, kThreads, 0, ex->stream>>>(
         (const int*)off, (const int*)list, d_nindex, (const int*)inl, (const int*)ioff_b, (const int*)itemv_b, nodes,
-        d_count, ex->d_ctl, d_graph_vptr, graphs, block_chunk, grab, &ex->d_ctl->hot[0]);
+        d_count, ex->d_ctl, d_graph_vptr, graphs, block_chunk, grab, &ex->d_ctl->hot[0], wl);
     tc_count_block<true, false><<<cgrid, kThreads, 0, ex->stream>>>(
         (const int*)off, (const int*)list, d_nindex, (const int*)inl, (const int*)ioff_b, (const int*)itemv_b, nodes,
-        d_count, ex->d_ctl, d_graph_vptr, graphs, block_chunk, grab, &ex->d_ctl->hot[kCtlSpread]);
+        d_count, ex->d_ctl, d_graph_vptr, graphs, block_chunk, grab, &ex->d_ctl->hot[kCtlSpread], wl);
     tc_count_warp<true><<<cgrid, kThreads, 0, ex->stream>>>((const int*)off, (const int*)list, d_nindex,
                                                             (const int*)inl, (const int*)ioff, (const int*)itemv,
-                                                            nodes, d_count, ex->d_ctl, d_graph_vptr, graphs);
+                                                            nodes, d_count, ex->d_ctl, d_graph_vptr, graphs, wl);
   } else {
     tc_count_block<false, true><<<cgrid, kThreads, 0, ex->stream>>>(
         (const int*)off, (const int*)list, d_nindex, (const int*)inl, (const int*)ioff_b, (const int*)itemv_b, nodes,
-        d_count, ex->d_ctl, nullptr, 0, block_chunk, grab, &ex->d_ctl->hot[0]);
+        d_count, ex->d_ctl, nullptr, 0, block_chunk, grab, &ex->d_ctl->hot[0], wl);
     tc_count_block<false, false><<<cgrid, kThreads, 0, ex->stream>>>(
         (const int*)off, (const int*)list, d_nindex, (const int*)inl, (const int*)ioff_b, (const int*)itemv_b, nodes,
-        d_count, ex->d_ctl, nullptr, 0, block_chunk, grab, &ex->d_ctl->hot[kCtlSpread]);
+        d_count, ex->d_ctl, nullptr, 0, block_chunk, grab, &ex->d_ctl->hot[kCtlSpread], wl);
     tc_count_warp<false><<<cgrid, kThreads, 0, ex->stream>>>((const int*)off, (const int*)list, d_nindex,
                                                              (const int*)inl, (const int*)ioff, (const int*)itemv,
-                                                             nodes, d_count, ex->d_ctl, nullptr, 0);
+                                                             nodes, d_count, ex->d_ctl, nullptr, 0, wl);
   }
   ig_count_launches(10);
   return ig_cuda_check((int)cudaGetLastError(), "tc launch");

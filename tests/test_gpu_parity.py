@@ -488,3 +488,19 @@ def test_tc_item_runs(ig, orc, graphs, grab):
     finally:
         ig.set_option("tc_grab", old[0])
         ig.set_option("tc_block_chunk", old[1])
+
+
+@pytest.mark.parametrize("warp_list", [1, 16, 33, 65, 97, 1 << 20])
+def test_tc_warp_walk_threshold(ig, orc, graphs, warp_list):
+    """Probe lists walked by the whole warp (128, 64 and 32 probes per step)
+    from a threshold of one probe up to none at all: the same counts, on the
+    plain and the degree-ordered ids, through the block and warp paths."""
+    old = ig.get_option("tc_warp_list")
+    try:
+        ig.set_option("tc_warp_list", warp_list)
+        for name in ("rmat14", "hubby", "complete", "star", "rmat18"):
+            for g in (graphs[name], graphs[name].degree_ordered()):
+                with ig.DeviceCSR(g) as d:
+                    assert ig.GPUtc_vertex(g.nodes, d.nindex_ptr, d.nlist_ptr)[0] == orc.tc(g), (name, warp_list)
+    finally:
+        ig.set_option("tc_warp_list", old)
