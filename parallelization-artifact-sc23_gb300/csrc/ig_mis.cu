@@ -18,14 +18,16 @@
 //     reaching the end includes it and pushes "excluded" to all neighbours;
 //   - statuses are updated in place (no per-round copy, unlike :89-103);
 //   - the undecided vertices are compacted into a worklist each round
-//     (warp-aggregated append), so later rounds touch only what is left;
+//     (staged per warp in shared memory, one atomic per 32 entries), so
+//     later rounds touch only what is left;
 //   - vertices with more than 32 neighbours are scanned 32 at a time by the
 //     whole warp with ballots;
-//   - warps take groups of 32-entry chunks from a per-round counter (the
-//     first group by warp index), so a run of high-degree vertices in
-//     consecutive ids (degree-ordered input) does not sit on a few warps; a
-//     group is up to 8 chunks, sized so every warp takes about 8 groups (few
-//     atomics on a long worklist).
+//   - groups of 32-entry chunks (up to 8 chunks, sized so every warp takes
+//     about 8 groups): the first static_pct percent dealt round-robin (no
+//     atomics), the rest taken one at a time from a per-round counter, so a
+//     run of high-degree vertices in consecutive ids (degree-ordered input)
+//     does not sit on a few warps and the counter is not hit by every
+//     group of the round.
 // The result equals the reference C++ CopyDeterm set bit for bit.  (The CUDA
 // variants compare priorities as signed int and reach a different set.)
 #include "ig_device.cuh"
@@ -46,6 +48,7 @@ struct MisArgs {
   int* wb;
   IgCtl* ctl;
   unsigned long long timeout_ns;
+  int static_pct;  // percent of a round's groups dealt round-robin
 };
 
 __device__ __forceinline__ int load_status(const int* s, int v) { return *((const volatile int*)s + v); }
@@ -63,6 +66,9 @@ __global__ void __launch_bounds__(kThreads) mis_persistent(MisArgs a) {
   const long long gtid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   const long long gthreads = (long long)gridDim.x * blockDim.x;
   const long long warp_g = gtid >> 5, nwarps = gthreads >> 5;
+  __shared__ int s_wbuf[kThreads / 32][kWarpBuf];  // per-warp staging of worklist appends
+  int* wbuf = s_wbuf[threadIdx.x >> 5];
+  int wbuf_n = 0;
 
   for (long long v = gtid; v < a.nodes; v += gthreads) {
     a.status[v] = kUndecided;
@@ -83,7 +89,15 @@ __global__ void __launch_bounds__(kThreads) mis_persistent(MisArgs a) {
     int* wsize = hot32(ctl, slot);
     int* grab = hot32(ctl, 3 + slot);
     const int gch = (int)max(1LL, min(8LL, (long long)cur_size / (nwarps * 256)));  // chunks per group
-    for (long long base0 = warp_g * 32 * gch; base0 < cur_size;) {
+    const long long ngroups = ((long long)cur_size + 32 * gch - 1) / (32 * gch);
+    const long long nstatic = max(min(ngroups, nwarps), ngroups * a.static_pct / 100);
+    long long grp = warp_g;
+    if (grp >= nstatic) {
+      long long nb = 0;
+      if (lane == 0) nb = nstatic + atomicAdd(grab, 1);
+      grp = __shfl_sync(IG_FULL, nb, 0);
+    }
+    for (long long base0 = grp * 32 * gch; grp < ngroups; base0 = grp * 32 * gch) {
       for (int sc = 0; sc < gch && base0 + 32 * sc < cur_size; sc++) {
         const long long base = base0 + 32 * sc;
         const long long i = base + lane;
@@ -157,12 +171,18 @@ __global__ void __launch_bounds__(kThreads) mis_persistent(MisArgs a) {
             if (lane == src_lane) blocked = true;
           }
         }
-        warp_append(blocked, v, nxt, wsize, a.nodes, ctl);
+        const int bv[1] = {v};
+        warp_buf_append<1>(blocked ? 1 : 0, bv, wbuf, wbuf_n, nxt, wsize, a.nodes, ctl);
       }
-      long long nb = 0;
-      if (lane == 0) nb = nwarps * 32 * gch + atomicAdd(grab, 32 * gch);
-      base0 = __shfl_sync(IG_FULL, nb, 0);
+      if (grp + nwarps < nstatic) {
+        grp += nwarps;
+      } else {
+        long long nb = 0;
+        if (lane == 0) nb = nstatic + atomicAdd(grab, 1);
+        grp = __shfl_sync(IG_FULL, nb, 0);
+      }
     }
+    warp_buf_flush(wbuf, wbuf_n, nxt, wsize, a.nodes, ctl);
     if (!grid_sync(ctl, a.timeout_ns, gb)) return;
     cur_size = ld_relaxed(wsize);
     round++;
@@ -185,7 +205,8 @@ int igk_mis(IgExec* ex, const ig_csr* dg, int* d_status, unsigned int* d_prio) {
   if ((rc = ig_scratch_get(ex->scratch, IG_SLOT_Q1, vb, &wb))) return rc;
   if ((rc = ig_exec_reset(ex))) return rc;
   const IgOptions& o = ig_exec_options(ex);
-  MisArgs a{dg->nindex, dg->nlist, dg->nodes, d_status, (int*)resume, (int*)wa, (int*)wb, ex->d_ctl, ex->timeout_ns};
+  MisArgs a{dg->nindex, dg->nlist,   dg->nodes,    d_status,       (int*)resume,
+            (int*)wa,   (int*)wb,    ex->d_ctl,    ex->timeout_ns, o.mis_static_pct};
   void* args[] = {&a};
   return ig_launch_coop(ex, (const void*)mis_persistent, kThreads, 0, o.blocks_per_sm, args, nullptr);
 }

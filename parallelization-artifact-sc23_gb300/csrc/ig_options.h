@@ -24,6 +24,9 @@ struct IgOptions {
                           // queue flags settled 32 at a time; 0 = settled by the step that found them
   int sssp_chunk;         // SSSP: frontier entries per warp chunk (1..32)
   int sssp_item_group;    // SSSP: most work-item slices a warp claims at a time (1..32)
+  int sssp_static_pct;    // SSSP: percent of a pass's frontier chunks and slice groups dealt round-robin
+                          // (no atomics); the rest are taken from a counter
+  int mis_static_pct;     // MIS: percent of a round's worklist groups dealt round-robin (no atomics)
   int pr_hub_degree;      // PageRank: degree above which a vertex is split in chunks
   int pr_chunk;           // PageRank: edges per hub chunk
   int pr_blocks_per_sm;   // PageRank: resident blocks per SM (0 = blocks_per_sm)

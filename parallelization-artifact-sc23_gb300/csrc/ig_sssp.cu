@@ -84,6 +84,7 @@ struct SsspArgs {
   int stage_flags;       // 1: improved vertices staged per warp, their queue flags settled 32 at a time
   int chunk;             // frontier entries per warp chunk (at most 32)
   int item_group;        // most work-item slices a warp takes at a time
+  int static_pct;        // share (percent) of a pass's chunks / slice groups dealt to warps without atomics
 };
 
 // Per-round counters: hot counters of the control block (every warp updates
@@ -334,7 +335,20 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) sssp_persistent(SsspArgs
       // small round's lists are spread over the whole grid.
       int* grab = ci(kCGrab + it % 3);
       const int cs = fcount >= nwarps * a.chunk ? a.chunk : max(1, (fcount + nwarps - 1) / nwarps);
-      for (int base = warp_g * cs; base < fcount;) {
+      // Chunk c holds entries [c * cs, (c + 1) * cs).  The first `nstatic`
+      // chunks are dealt round-robin (warp w takes w, w + nwarps, ...), the
+      // rest taken one at a time from the round's counter: one counter that
+      // every warp of the grid hits saturates near 300M atomics/s, so only
+      // the tail of the pass, where the balance matters, uses it.
+      const int nchunks = (fcount + cs - 1) / cs;
+      const int nstatic = max(min(nchunks, nwarps), (int)((long long)nchunks * a.static_pct / 100));
+      int chunk_id = warp_g;
+      if (chunk_id >= nstatic) {
+        int nb = 0;
+        if (lane == 0) nb = nstatic + atomicAdd(grab, 1);
+        chunk_id = __shfl_sync(IG_FULL, nb, 0);
+      }
+      for (int base = chunk_id * cs; chunk_id < nchunks; base = chunk_id * cs) {
         const int i = base + lane;
         int u = 0, beg = 0, deg = 0, du = kInf;
         bool expand = false, defer = false;
@@ -443,9 +457,13 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) sssp_persistent(SsspArgs
             }
           }
         }
-        int nb = 0;
-        if (lane == 0) nb = nwarps * cs + atomicAdd(grab, cs);
-        base = __shfl_sync(IG_FULL, nb, 0);
+        if (chunk_id + nwarps < nstatic) {
+          chunk_id += nwarps;
+        } else {
+          int nb = 0;
+          if (lane == 0) nb = nstatic + atomicAdd(grab, 1);
+          chunk_id = __shfl_sync(IG_FULL, nb, 0);
+        }
       }
       // Work items (vertex, chunk of item_edges edges) are cut in slices of
       // kSlice edges, 2^slog slices per item (the last ones of a short chunk
@@ -490,7 +508,18 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) sssp_persistent(SsspArgs
       auto barrier_items = [&](const unsigned long long* list, int nm, unsigned long long* cnt) {
         const long long units = (long long)nm << slog;
         const int g = (int)min((long long)a.item_group, max(1LL, units / (4LL * nwarps)));
-        for (long long j0 = (long long)warp_g * g; j0 < units;) {
+        // group q holds slices [q * g, (q + 1) * g): the first nsg dealt
+        // round-robin, the rest taken from the counter (as the frontier chunks)
+        const long long ngroups = (units + g - 1) / g;
+        const long long nsg = max(min(ngroups, (long long)nwarps), ngroups * a.static_pct / 100);
+        long long q = warp_g;
+        if (q >= nsg) {
+          unsigned long long nb = 0;
+          if (lane == 0) nb = (unsigned long long)nsg + atomicAdd(cnt, 1ull);
+          q = (long long)__shfl_sync(IG_FULL, nb, 0);
+        }
+        for (; q < ngroups;) {
+          const long long j0 = q * g;
           const long long j1 = min(j0 + g, units);
           const int mfirst = (int)(j0 >> slog);
           const int ni = (int)((j1 - 1) >> slog) - mfirst + 1;
@@ -505,9 +534,13 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) sssp_persistent(SsspArgs
             hd = min(a.item_edges, d0 - off0);
           }
           expand_slices(j0, j1, mfirst, hdu, hb, hd);
-          unsigned long long nb = 0;
-          if (lane == 0) nb = (unsigned long long)nwarps * g + atomicAdd(cnt, (unsigned long long)g);
-          j0 = (long long)__shfl_sync(IG_FULL, nb, 0);
+          if (q + nwarps < nsg) {
+            q += nwarps;
+          } else {
+            unsigned long long nb = 0;
+            if (lane == 0) nb = (unsigned long long)nsg + atomicAdd(cnt, 1ull);
+            q = (long long)__shfl_sync(IG_FULL, nb, 0);
+          }
         }
       };
       auto end_pass = [&]() {
@@ -712,7 +745,7 @@ int igk_sssp(IgExec* ex, const ig_csr* dg, int src, int* d_dist) {
              (int*)expanded, (int*)members, (int*)inmember, ex->d_ctl, ex->timeout_ns, o.sssp_item_edges,
              o.sssp_warp_degree,
              o.sssp_delta, o.sssp_delta_scale, o.sssp_heavy_split, o.sssp_window_scale,
-             o.sssp_window_degree, o.sssp_merge_below, o.sssp_spin_ns, o.sssp_stage_flags, o.sssp_chunk, o.sssp_item_group};
+             o.sssp_window_degree, o.sssp_merge_below, o.sssp_spin_ns, o.sssp_stage_flags, o.sssp_chunk, o.sssp_item_group, o.sssp_static_pct};
   void* args[] = {&a};
   // the register budget follows the residency cap (4, 5 or 6 blocks of 256 threads per SM)
   // (the paired-slice form holds more registers: 3 blocks per SM, or 4 with spills)

@@ -504,3 +504,32 @@ def test_tc_warp_walk_threshold(ig, orc, graphs, warp_list):
                     assert ig.GPUtc_vertex(g.nodes, d.nindex_ptr, d.nlist_ptr)[0] == orc.tc(g), (name, warp_list)
     finally:
         ig.set_option("tc_warp_list", old)
+
+
+@pytest.mark.parametrize("pct", [0, 75, 100])
+def test_static_share_forms(ig, orc, graphs, pct):
+    """Frontier chunks, work-item slice groups (SSSP) and worklist groups
+    (MIS) dealt round-robin up to a share of the pass, the rest taken from
+    the counter: exact distances and the reference's set, with one- and
+    two-slice work items, on the plain and the degree-ordered ids."""
+    names = ("sssp_static_pct", "mis_static_pct", "sssp_item_edges", "sssp_warp_degree")
+    old = {k: ig.get_option(k) for k in names}
+    try:
+        ig.set_option("sssp_static_pct", pct)
+        ig.set_option("mis_static_pct", pct)
+        for ie, wd in ((128, 64), (256, 4)):
+            ig.set_option("sssp_item_edges", ie)
+            ig.set_option("sssp_warp_degree", wd)
+            for name in ("rmat14", "hubby", "road128", "star", "rmat18"):
+                for g in (graphs[name], graphs[name].degree_ordered()):
+                    with ig.DeviceCSR(g) as d:
+                        for s in (0, g.nodes // 2):
+                            dist = np.empty(g.nodes, np.int32)
+                            ig.GPUsssp_vertex(int(s), d, dist)
+                            assert np.array_equal(dist, orc.sssp(g, int(s))), (name, s, ie)
+                        st = np.empty(g.nodes, np.int32)
+                        ig.GPUmis_vertex(d, None, st)
+                        assert np.array_equal(st, orc.mis(g).astype(np.int32)), name
+    finally:
+        for k, v in old.items():
+            ig.set_option(k, v)
