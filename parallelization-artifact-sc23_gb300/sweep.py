@@ -49,14 +49,19 @@ BIG = 1 << 30
 #        work items (default); order: Window = long lists expanded near
 #        Dijkstra order, NoWindow; sync: Sync2 = work items after a second
 #        grid barrier per round, Sync1 = within the round (one barrier);
-#        Plain / LightHeavy edge split.  (Always a data-driven worklist.)
+#        Plain / LightHeavy edge split; flags: Staged = improved vertices'
+#        queue flags settled 32 at a time, Immediate = by the step that found
+#        them; schedule: Static75 = the first 75% of a pass's chunks dealt
+#        round-robin, Dynamic = all but the first per warp from a counter.
+#        (Always a data-driven worklist.)
 #   CC   link: BfsSeed = the largest-degree vertex's component labelled by
 #        a BFS from it (direction-optimising traversal), union-find for the
 #        rest; Pass = neighbour sampling (two neighbours linked in one pass
 #        with path halving), Rounds = one round per sampled neighbour with a
 #        compression after each, FlatPass = Pass after flattening the initial
 #        forest; granularity as BFS.  (Hooking pushes along edges.)
-#   MIS  residency only (B4 / B2 / B8 blocks per SM).
+#   MIS  residency (B4 / B2 / B8 blocks per SM); schedule: Dynamic worklist
+#        groups from a counter, Static75 = 75% dealt round-robin.
 #   PR   gather: OnePass = contributions gathered while summing, TwoPass =
 #        every edge's contribution gathered first in one dense pass (measured
 #        slower: the gathers cost the same either way); granularity: WarpPair
@@ -65,7 +70,9 @@ BIG = 1 << 30
 #        4096 / 256 edges; Prefetch / NoPrefetch of each warp's next lists.
 #        (Pull only: push PageRank needs float atomics, not deterministic.)
 #   TC   block work items of 4096 / 1024 in-neighbours, taken by blocks in
-#        runs of 2 or 4 from a counter or dealt in a grid stride.
+#        runs of 2 or 4 from a counter or dealt in a grid stride; walk: probe
+#        lists from 64 (Walk64) or 96 (Walk96) probes walked by the whole
+#        warp, or every list through the owner search (Owner).
 STYLES = {
     "bfs": {"direction": {"PushPull": {}, "Push": {"bfs_alpha": 0}, "Pull": {"bfs_alpha": 1000000}},
             "granularity": {"WarpGrid": {}, "Warp": {"hub_degree": BIG}, "Grid": {"hub_degree": 32}},
@@ -73,17 +80,21 @@ STYLES = {
     "sssp": {"parallel": {"VE": {}, "V": {"sssp_warp_degree": BIG}, "E": {"sssp_warp_degree": 1}},
              "order": {"Window": {}, "NoWindow": {"sssp_window_scale": 0}},
              "sync": {"Sync2": {}, "Sync1": {"sssp_merge_below": BIG}},
-             "split": {"Plain": {}, "LightHeavy": {"sssp_heavy_split": 1}}},
+             "split": {"Plain": {}, "LightHeavy": {"sssp_heavy_split": 1}},
+             "flags": {"Staged": {}, "Immediate": {"sssp_stage_flags": 0}},
+             "schedule": {"Static75": {}, "Dynamic": {"sssp_static_pct": 0}}},
     "cc": {"link": {"BfsSeed": {}, "Pass": {"cc_bfs_seed": 0}, "Rounds": {"cc_bfs_seed": 0, "cc_rounds": 1},
                     "FlatPass": {"cc_bfs_seed": 0, "cc_rounds": 2}},
            "granularity": {"WarpGrid": {}, "Grid": {"hub_degree": 64}, "Warp": {"hub_degree": BIG}}},
-    "mis": {"residency": {"B4": {}, "B2": {"blocks_per_sm": 2}, "B8": {"blocks_per_sm": 8}}},
+    "mis": {"residency": {"B4": {}, "B2": {"blocks_per_sm": 2}, "B8": {"blocks_per_sm": 8}},
+            "schedule": {"Dynamic": {}, "Static75": {"mis_static_pct": 75}}},
     "pr": {"gather": {"OnePass": {}, "TwoPass": {"pr_two_pass": 1}},
            "granularity": {"WarpPair": {}, "SubWarp": {"pr_subwarp": 1}},
            "hubs": {"Chunk1024": {}, "Chunk4096": {"pr_hub_degree": 4096}, "Chunk256": {"pr_hub_degree": 256}},
            "prefetch": {"Prefetch": {}, "NoPrefetch": {"pr_prefetch": 0}}},
     "tc": {"items": {"Item4096": {}, "Item1024": {"tc_block_chunk": 1024}},
-           "schedule": {"Runs2": {}, "Stride": {"tc_grab": 0}, "Runs4": {"tc_grab": 4}}},
+           "schedule": {"Runs2": {}, "Stride": {"tc_grab": 0}, "Runs4": {"tc_grab": 4}},
+           "walk": {"Walk64": {}, "Walk96": {"tc_warp_list": 96}, "Owner": {"tc_warp_list": 1 << 20}}},
 }
 AXES = STYLES  # the per-algorithm axes (name kept for callers)
 OPTION_NAMES = sorted({k for axes in STYLES.values() for words in axes.values() for o in words.values() for k in o})

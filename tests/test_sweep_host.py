@@ -33,7 +33,8 @@ def test_style_words_name_the_axes():
     names = [sweep.variant_name("rmat20", a, w) for a in sweep.STYLES for w, _ in sweep.variants(a)]
     assert len(names) == len(set(names))
     assert "rmat20_gb300_BFS_GB300_Pull_WarpGrid_Bitmap.cu" in names
-    assert "rmat20_gb300_SSSP_GB300_E_Window_Sync2_Plain.cu" in names
+    assert "rmat20_gb300_SSSP_GB300_E_Window_Sync2_Plain_Staged_Static75.cu" in names
+    assert "rmat20_gb300_TC_GB300_Item4096_Runs2_Owner.cu" in names
 
 
 def test_csv_round_trip(tmp_path):
