@@ -379,6 +379,24 @@ __device__ __forceinline__ int block_scan_int(int x, int* tmp, int* total) {
   return res;
 }
 
+// Block-wide sum of 64-bit integers (exact); the result is valid in thread 0.
+// `tmp` must hold 32 values.
+__device__ __forceinline__ unsigned long long block_sum_u64(unsigned long long x, unsigned long long* tmp) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(IG_FULL, x, o);
+  __syncthreads();
+  if (lane == 0) tmp[warp] = x;
+  __syncthreads();
+  unsigned long long r = 0;
+  if (warp == 0) {
+    r = (lane < nw) ? tmp[lane] : 0ull;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) r += __shfl_down_sync(IG_FULL, r, o);
+  }
+  return r;
+}
+
 // Block-wide sum of a double with a fixed reduction tree (deterministic);
 // the result is valid in thread 0.  `tmp` must hold 32 doubles.
 __device__ __forceinline__ double block_sum_double(double x, double* tmp) {

@@ -26,12 +26,15 @@ struct IgOptions {
   int sssp_item_group;    // SSSP: most work-item slices a warp claims at a time (1..32)
   int sssp_static_pct;    // SSSP: percent of a pass's frontier chunks and slice groups dealt round-robin
                           // (no atomics); the rest are taken from a counter
+  int sssp_tail_split;    // SSSP: chunks / slice groups taken from the counter are this many times smaller
+  int sssp_claim_ahead;   // SSSP: 1 = a warp claims its next chunk from the counter as it starts the current
   int mis_static_pct;     // MIS: percent of a round's worklist groups dealt round-robin (no atomics)
   int pr_hub_degree;      // PageRank: degree above which a vertex is split in chunks
   int pr_chunk;           // PageRank: edges per hub chunk
   int pr_blocks_per_sm;   // PageRank: resident blocks per SM (0 = blocks_per_sm)
   int pr_prefetch;        // PageRank: 1 = a warp prefetches its next lists into L2 while summing
   int pr_subwarp;         // PageRank: 1 = medium lists summed four at a time by 8-lane sub-warps
+  int pr_static_pct;      // PageRank: percent of the vertex groups dealt round-robin, the rest from a counter
   int pr_two_pass;        // PageRank: 1 = each iteration first gathers every edge's contribution in one
                           // dense pass (128-bit loads and stores), then sums the lists from it
   int tc_block_chunk;     // TC: in-neighbours per block work item

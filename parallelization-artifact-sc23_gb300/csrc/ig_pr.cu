@@ -14,14 +14,24 @@
 //
 // Accuracy: each vertex's incoming sum is accumulated in FP32 with Kahan
 // compensation (lanes of a warp combine their partial sums exactly with
-// TwoSum); the residual is accumulated in FP64 with a fixed reduction tree,
-// so every run of the same input gives bit-identical scores.
+// TwoSum); each vertex's |change| is rounded once to a 64-bit fixed-point
+// integer (units of 2^-60) and the residual is their integer sum, exact in
+// any order, so every run of the same input gives bit-identical scores and
+// the same iteration count however the vertices were dealt to warps.  (A
+// batched run stops each graph on its own FP64 residual.)
 //
-// Work split: 32 consecutive vertices per warp (static schedule).  A vertex
+// Work split: groups of 32 consecutive vertices, the first static_pct
+// percent of them dealt round-robin to the warps and the rest taken one at
+// a time from a per-iteration counter (claimed one group ahead, so the
+// claim's round trip and the next group's list loads overlap the current
+// group's sums); a list's cost varies with its degree, so the counter
+// evens out the end of the iteration.  A vertex
 // with <= kLight neighbours is summed by its own lane, one with more by the
 // whole warp; a vertex above the hub degree is cut into fixed chunks of edges
 // spread over all warps, and its chunk sums are combined in chunk order after
 // a grid barrier.
+#include <type_traits>
+
 #include "ig_device.cuh"
 #include "ig_options.h"
 
@@ -44,7 +54,7 @@ struct PrArgs {
   int* chunk_hub;     // hub index of each chunk
   float2* partial;    // per-chunk (hi, lo) sums
   int* blk;           // per-block counts for the deterministic hub compaction (2 * grid)
-  double* blkerr;     // per-block residual partials (2 * grid)
+  unsigned long long* blkerr;  // per-block residual partials, fixed point (2 * grid)
   IgCtl* ctl;
   float eps;
   int max_iter;
@@ -63,7 +73,17 @@ struct PrArgs {
   double* gres;
   int* giters;
   int* vgraph;  // graph of every vertex (filled by the kernel before the first iteration)
+  int static_pct;  // percent of the vertex groups dealt round-robin (the rest from a counter)
 };
+
+constexpr double kFix = 1152921504606846976.0;  // 2^60: residual fixed-point scale
+constexpr int kPrGrab = 0;                       // hot counters kPrGrab + it % 3: groups claimed in iteration it
+
+// |change| of one score in fixed point: a graph's scores sum to at most 1,
+// so its changes sum to at most 2 and the total stays below 2^61.  (The
+// batched form, whose graphs stop on their own residuals, keeps the total in
+// double: it is only reported.)
+__device__ __forceinline__ unsigned long long pr_fixed(double x) { return __double2ull_rn(x * kFix); }
 
 // Adds each lane's x into gres[g_lane] with one atomic per distinct graph of the warp.
 __device__ __forceinline__ void warp_add_by_graph(double* gres, int g, double x, bool valid) {
@@ -238,7 +258,12 @@ template <bool kBatched, bool kTwo>
 __global__ void __launch_bounds__(kThreads, 4) pr_persistent(PrArgs a) {
   using namespace ig;
   __shared__ int s_scan[33];
-  __shared__ double s_red[32];
+  __shared__ unsigned long long s_red[32];
+  using Err = typename std::conditional<kBatched, double, unsigned long long>::type;
+  auto fix = [](double x) -> Err {
+    if constexpr (kBatched) return x;
+    else return pr_fixed(x);
+  };
   IgCtl* ctl = a.ctl;
   GridBar gb;  // this block's view of the barrier generation
   const int lane = lane_id();
@@ -322,7 +347,10 @@ __global__ void __launch_bounds__(kThreads, 4) pr_persistent(PrArgs a) {
   double residual = 0;
   while (it < a.max_iter) {
     it++;
-    double err = 0;
+    Err err = 0;  // this thread's |changes| (fixed point, but for the batched form)
+    // groups claimed in this iteration; the counter of the next one is reset here
+    unsigned long long* grab = hot64(ctl, kPrGrab + it % 3);
+    if (gtid == 0) *hot64(ctl, kPrGrab + (it + 1) % 3) = 0;
     // batched: a graph whose residual fell below epsilon stops changing (its
     // scores are final after that iteration, as for a single-graph run)
     double* gcur = kBatched ? a.gres + (it % 3) * a.graphs : nullptr;
@@ -371,30 +399,40 @@ __global__ void __launch_bounds__(kThreads, 4) pr_persistent(PrArgs a) {
       warp_gather_sum<kTwo>(a.nlist, kTwo ? a.vals : cur, b, e, shi, slo);
       if (lane == 0) a.partial[c] = make_float2(shi, slo);
     }
-    // each lane's list range of the warp's next group is loaded (and its list
-    // prefetched into L2) while the current group is summed
-    int nb = 0, ne = 0;
-    {
-      const long long v0 = (long long)warp_g * 32 + lane;
-      if (v0 < a.nodes) {
-        nb = __ldg(&a.nindex[v0]);
-        ne = __ldg(&a.nindex[v0 + 1]);
-        if (a.prefetch && ne - nb <= a.hub_degree) prefetch_list(a, kTwo ? (const void*)a.vals : a.nlist, nb, ne);
+    // Vertex groups: this warp's sequence is warp_g, warp_g + nwarps, ...
+    // below nstatic, then groups claimed from the counter.  Each lane's list
+    // range of the warp's next group is loaded (and its list prefetched into
+    // L2), and the group after it claimed, while the current group is summed.
+    const long long ngroups = ((long long)a.nodes + 31) >> 5;
+    const long long nstatic = max(min(ngroups, (long long)nwarps), ngroups * a.static_pct / 100);
+    auto load_ranges = [&](long long grp, int& rb, int& re) {
+      const long long vn = grp * 32 + lane;
+      rb = re = 0;
+      if (grp < ngroups && vn < a.nodes) {
+        rb = __ldg(&a.nindex[vn]);
+        re = __ldg(&a.nindex[vn + 1]);
+        if (a.prefetch && re - rb <= a.hub_degree) prefetch_list(a, kTwo ? (const void*)a.vals : a.nlist, rb, re);
       }
+    };
+    long long grp = warp_g, gnext;
+    if (grp + nwarps < nstatic) {
+      gnext = grp + nwarps;
+    } else {
+      unsigned long long c = 0;
+      if (lane == 0) c = (unsigned long long)nstatic + atomicAdd(grab, 1ull);
+      gnext = (long long)__shfl_sync(IG_FULL, c, 0);
     }
-    for (long long base = (long long)warp_g * 32; base < a.nodes; base += (long long)nwarps * 32) {
-      const long long vi = base + lane;
+    int nb = 0, ne = 0;
+    load_ranges(grp, nb, ne);
+    while (grp < ngroups) {
+      const long long vi = grp * 32 + lane;
       int v = (int)vi;
       const int b = nb, e = ne;
-      {
-        const long long vn = vi + (long long)nwarps * 32;
-        nb = ne = 0;
-        if (vn < a.nodes) {
-          nb = __ldg(&a.nindex[vn]);
-          ne = __ldg(&a.nindex[vn + 1]);
-          if (a.prefetch && ne - nb <= a.hub_degree) prefetch_list(a, kTwo ? (const void*)a.vals : a.nlist, nb, ne);
-        }
-      }
+      // the group after gnext: static, or claimed now (used at the end)
+      const bool claim = gnext < ngroups && gnext + nwarps >= nstatic;
+      unsigned long long claimed = 0;
+      if (claim && lane == 0) claimed = (unsigned long long)nstatic + atomicAdd(grab, 1ull);
+      load_ranges(gnext, nb, ne);
       int d = e - b;
       float sum = 0.f;
       int vg = 0;
@@ -471,9 +509,11 @@ __global__ void __launch_bounds__(kThreads, 4) pr_persistent(PrArgs a) {
         a.scores[v] = nw;
         nxt[v] = __fdiv_rn(nw, (float)vdegree(a, v));
         verr = (double)fabsf(__fsub_rn(nw, old));
-        err += verr;
+        err += fix(verr);
       }
       if (kBatched) warp_add_by_graph(gcur, vg, verr, upd);
+      grp = gnext;
+      gnext = claim ? (long long)__shfl_sync(IG_FULL, claimed, 0) : gnext + nwarps;
     }
     // ---- phase B: combine hub chunks in chunk order
     if (nh > 0) {
@@ -502,25 +542,34 @@ __global__ void __launch_bounds__(kThreads, 4) pr_persistent(PrArgs a) {
           a.scores[v] = nw;
           nxt[v] = __fdiv_rn(nw, (float)vdegree(a, v));
           const double herr = (double)fabsf(__fsub_rn(nw, old));
-          err += herr;
+          err += fix(herr);
           if (kBatched && herr != 0.0) atomicAdd(&gcur[hg], herr);
         }
       }
     }
-    const double berr = block_sum_double(err, s_red);
-    double* slot = a.blkerr + (it & 1) * G;
+    // block partial: integer (or the batched form's double, as bits)
+    unsigned long long berr;
+    if constexpr (kBatched) berr = (unsigned long long)__double_as_longlong(block_sum_double(err, (double*)s_red));
+    else berr = block_sum_u64(err, s_red);
+    unsigned long long* slot = a.blkerr + (it & 1) * G;
     if (threadIdx.x == 0) slot[blockIdx.x] = berr;
     if (!grid_sync(ctl, a.timeout_ns, gb)) return;
-    // the grid's residual: warp 0 of every block sums the block partials with
-    // the same fixed tree (lane-strided sums, then a shuffle tree), so every
-    // block reaches the same value and the same stop decision
+    // the grid's residual: warp 0 of every block sums the block partials
+    // (integers: the same total in every block, whatever the order)
     __shared__ double s_res;
     if (threadIdx.x < 32) {
-      double r = 0.0;
-      for (int b = threadIdx.x; b < G; b += 32) r += ld_relaxed(&slot[b]);
+      Err r = 0;
+      for (int b = threadIdx.x; b < G; b += 32) {
+        const unsigned long long x = ld_relaxed(&slot[b]);
+        if constexpr (kBatched) r += __longlong_as_double((long long)x);
+        else r += x;
+      }
 #pragma unroll
       for (int o = 16; o > 0; o >>= 1) r += __shfl_xor_sync(IG_FULL, r, o);
-      if (threadIdx.x == 0) s_res = r;
+      if (threadIdx.x == 0) {
+        if constexpr (kBatched) s_res = r;
+        else s_res = (double)r / kFix;
+      }
     }
     __syncthreads();
     residual = s_res;
@@ -591,9 +640,9 @@ static int pr_launch(IgExec* ex, const ig_csr* dg, const int* d_degree, float* d
   const float damp = 0.85f;
   const float base = (1.0f - damp) / (float)n;
   PrArgs a{dg->nindex, dg->nlist, d_degree, n, dg->edges, d_scores, (float*)ca, (float*)cb, (int*)hubs,
-           (int*)cbase, (int*)chub, (float2*)part, (int*)blk, (double*)blkerr, ex->d_ctl, epsilon, max_iter, base, damp,
+           (int*)cbase, (int*)chub, (float2*)part, (int*)blk, (unsigned long long*)blkerr, ex->d_ctl, epsilon, max_iter, base, damp,
            ex->timeout_ns, hub_degree, chunk, o.pr_prefetch, o.pr_subwarp, (float*)vals, d_graph_vptr, graphs,
-           (double*)gres, d_iters, (int*)vgraph};
+           (double*)gres, d_iters, (int*)vgraph, o.pr_static_pct};
   void* args[] = {&a};
   const int bps = o.pr_blocks_per_sm > 0 ? o.pr_blocks_per_sm : o.blocks_per_sm;
   const int cap = bps > 0 ? std::min(bps, 32) : 32;

@@ -85,6 +85,8 @@ struct SsspArgs {
   int chunk;             // frontier entries per warp chunk (at most 32)
   int item_group;        // most work-item slices a warp takes at a time
   int static_pct;        // share (percent) of a pass's chunks / slice groups dealt to warps without atomics
+  int tail_split;        // chunks / slice groups taken from the counter are this many times smaller
+  int claim_ahead;       // 1: a warp claims its next chunk from the counter when it starts the current one
 };
 
 // Per-round counters: hot counters of the control block (every warp updates
@@ -328,31 +330,46 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) sssp_persistent(SsspArgs
         }
         warp_buf_append2_flags<N>(v, tn, nbuf, nbuf_n, nxt, qsize, tf, fbuf, fbuf_n, far, fsize, a.nodes, ctl);
       };
-      // first chunk by warp index, the rest taken from a per-round counter so
-      // that warps that drew light chunks take more (the round ends at the
-      // grid barrier, so the slowest warp sets its length).  A chunk is 32
-      // queue entries, fewer when the queue has less than 32 per warp, so a
-      // small round's lists are spread over the whole grid.
+      // Frontier chunks: a chunk is 32 queue entries, fewer when the queue
+      // has less than 32 per warp, so a small round's lists are spread over
+      // the whole grid.  The first `nstatic` chunks are dealt round-robin
+      // (warp w takes w, w + nwarps, ...); the rest of the queue is taken
+      // from the round's counter in chunks of cs / tail_split entries, so
+      // warps that drew light chunks take more and the pass ends evenly (the
+      // round ends at the grid barrier, so the slowest warp sets its length).
+      // A claim from the counter is a round trip on the warp's critical
+      // path; with claim_ahead the next chunk is claimed when the current
+      // one starts.
       int* grab = ci(kCGrab + it % 3);
       const int cs = fcount >= nwarps * a.chunk ? a.chunk : max(1, (fcount + nwarps - 1) / nwarps);
-      // Chunk c holds entries [c * cs, (c + 1) * cs).  The first `nstatic`
-      // chunks are dealt round-robin (warp w takes w, w + nwarps, ...), the
-      // rest taken one at a time from the round's counter: one counter that
-      // every warp of the grid hits saturates near 300M atomics/s, so only
-      // the tail of the pass, where the balance matters, uses it.
       const int nchunks = (fcount + cs - 1) / cs;
       const int nstatic = max(min(nchunks, nwarps), (int)((long long)nchunks * a.static_pct / 100));
-      int chunk_id = warp_g;
-      if (chunk_id >= nstatic) {
-        int nb = 0;
-        if (lane == 0) nb = nstatic + atomicAdd(grab, 1);
-        chunk_id = __shfl_sync(IG_FULL, nb, 0);
+      const int dyn_base = min(fcount, nstatic * cs);  // first entry of the counter's part
+      const int csd = max(1, cs / a.tail_split);       // entries per claimed chunk
+      auto dyn_chunk = [&](int k, int& start, int& len) {
+        start = dyn_base + k * csd;
+        len = max(0, min(csd, fcount - start));
+      };
+      int sc = warp_g;  // static chunk index; -1 once in the counter's part
+      int start = 0, len = 0;
+      if (sc < nstatic) {
+        start = sc * cs;
+        len = min(cs, fcount - start);
+      } else {
+        sc = -1;
+        int k = 0;
+        if (lane == 0) k = atomicAdd(grab, 1);
+        dyn_chunk(__shfl_sync(IG_FULL, k, 0), start, len);
       }
-      for (int base = chunk_id * cs; chunk_id < nchunks; base = chunk_id * cs) {
+      while (len > 0) {
+        const bool next_static = sc >= 0 && sc + nwarps < nstatic;
+        int ahead = 0;
+        if (!next_static && a.claim_ahead && lane == 0) ahead = atomicAdd(grab, 1);
+        const int base = start;
         const int i = base + lane;
         int u = 0, beg = 0, deg = 0, du = kInf;
         bool expand = false, defer = false;
-        if (lane < cs && i < fcount) {
+        if (lane < len) {
           u = frontier[i];
           // every per-vertex read depends only on u, so they are issued together
           du = a.dist[u];
@@ -457,12 +474,14 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) sssp_persistent(SsspArgs
             }
           }
         }
-        if (chunk_id + nwarps < nstatic) {
-          chunk_id += nwarps;
+        if (next_static) {
+          sc += nwarps;
+          start = sc * cs;
+          len = min(cs, fcount - start);
         } else {
-          int nb = 0;
-          if (lane == 0) nb = nstatic + atomicAdd(grab, 1);
-          chunk_id = __shfl_sync(IG_FULL, nb, 0);
+          sc = -1;
+          if (!a.claim_ahead && lane == 0) ahead = atomicAdd(grab, 1);
+          dyn_chunk(__shfl_sync(IG_FULL, ahead, 0), start, len);
         }
       }
       // Work items (vertex, chunk of item_edges edges) are cut in slices of
@@ -509,18 +528,27 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) sssp_persistent(SsspArgs
         const long long units = (long long)nm << slog;
         const int g = (int)min((long long)a.item_group, max(1LL, units / (4LL * nwarps)));
         // group q holds slices [q * g, (q + 1) * g): the first nsg dealt
-        // round-robin, the rest taken from the counter (as the frontier chunks)
+        // round-robin, the rest taken from the counter in groups of
+        // g / tail_split slices (as the frontier chunks)
         const long long ngroups = (units + g - 1) / g;
         const long long nsg = max(min(ngroups, (long long)nwarps), ngroups * a.static_pct / 100);
-        long long q = warp_g;
-        if (q >= nsg) {
-          unsigned long long nb = 0;
-          if (lane == 0) nb = (unsigned long long)nsg + atomicAdd(cnt, 1ull);
-          q = (long long)__shfl_sync(IG_FULL, nb, 0);
+        const long long dbase = min(units, nsg * g);
+        const int gd = max(1, g / a.tail_split);
+        long long q = warp_g, j0 = 0, j1 = 0;
+        if (q < nsg) {
+          j0 = q * g;
+          j1 = min(j0 + g, units);
+        } else {
+          q = -1;
+          unsigned long long k = 0;
+          if (lane == 0) k = atomicAdd(cnt, 1ull);
+          j0 = dbase + (long long)__shfl_sync(IG_FULL, k, 0) * gd;
+          j1 = min(j0 + gd, units);
         }
-        for (; q < ngroups;) {
-          const long long j0 = q * g;
-          const long long j1 = min(j0 + g, units);
+        while (j0 < j1) {
+          const bool next_static = q >= 0 && q + nwarps < nsg;
+          unsigned long long ahead = 0;
+          if (!next_static && a.claim_ahead && lane == 0) ahead = atomicAdd(cnt, 1ull);
           const int mfirst = (int)(j0 >> slog);
           const int ni = (int)((j1 - 1) >> slog) - mfirst + 1;
           int hdu = kInf, hb = 0, hd = 0;
@@ -534,12 +562,15 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) sssp_persistent(SsspArgs
             hd = min(a.item_edges, d0 - off0);
           }
           expand_slices(j0, j1, mfirst, hdu, hb, hd);
-          if (q + nwarps < nsg) {
+          if (next_static) {
             q += nwarps;
+            j0 = q * g;
+            j1 = min(j0 + g, units);
           } else {
-            unsigned long long nb = 0;
-            if (lane == 0) nb = (unsigned long long)nsg + atomicAdd(cnt, 1ull);
-            q = (long long)__shfl_sync(IG_FULL, nb, 0);
+            q = -1;
+            if (!a.claim_ahead && lane == 0) ahead = atomicAdd(cnt, 1ull);
+            j0 = dbase + (long long)__shfl_sync(IG_FULL, ahead, 0) * gd;
+            j1 = min(j0 + gd, units);
           }
         }
       };
@@ -745,7 +776,7 @@ int igk_sssp(IgExec* ex, const ig_csr* dg, int src, int* d_dist) {
              (int*)expanded, (int*)members, (int*)inmember, ex->d_ctl, ex->timeout_ns, o.sssp_item_edges,
              o.sssp_warp_degree,
              o.sssp_delta, o.sssp_delta_scale, o.sssp_heavy_split, o.sssp_window_scale,
-             o.sssp_window_degree, o.sssp_merge_below, o.sssp_spin_ns, o.sssp_stage_flags, o.sssp_chunk, o.sssp_item_group, o.sssp_static_pct};
+             o.sssp_window_degree, o.sssp_merge_below, o.sssp_spin_ns, o.sssp_stage_flags, o.sssp_chunk, o.sssp_item_group, o.sssp_static_pct, o.sssp_tail_split, o.sssp_claim_ahead};
   void* args[] = {&a};
   // the register budget follows the residency cap (4, 5 or 6 blocks of 256 threads per SM)
   // (the paired-slice form holds more registers: 3 blocks per SM, or 4 with spills)

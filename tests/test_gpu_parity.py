@@ -533,3 +533,26 @@ def test_static_share_forms(ig, orc, graphs, pct):
     finally:
         for k, v in old.items():
             ig.set_option(k, v)
+
+
+def test_pagerank_schedule_independent(ig, orc, graphs):
+    """Vertex groups dealt round-robin (100%), partly (75%, 50%) or all from
+    the counter (0%): the same scores bit for bit and the same iteration
+    count -- each vertex's sum depends only on its list and the residual is
+    an exact integer sum -- and within 1e-6 relative L1 of FP64."""
+    old = ig.get_option("pr_static_pct")
+    try:
+        for name in ("rmat14", "hubby", "road128", "rmat18"):
+            g = graphs[name]
+            outs = []
+            for pct in (100, 75, 50, 0):
+                ig.set_option("pr_static_pct", pct)
+                s = np.full(g.nodes, np.float32(1.0) / np.float32(g.nodes), np.float32)
+                it, _ = ig.PR_GPU(g, s, g.degree(), 1e-6, 100)
+                outs.append((it, s))
+            for it, s in outs[1:]:
+                assert it == outs[0][0] and np.array_equal(s, outs[0][1]), name
+            ref, _, _ = orc.pr_f64(g, iters=outs[0][0])
+            assert np.abs(outs[0][1] - ref).sum() / ref.sum() <= PR_TOL, name
+    finally:
+        ig.set_option("pr_static_pct", old)
