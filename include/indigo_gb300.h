@@ -144,7 +144,7 @@ int ig_event_elapsed_ms(void* start, void* stop, float* ms);
 /* Bound (milliseconds) on every device-side wait; default 5000. */
 int ig_set_wait_timeout_ms(int ms);
 /* Kernel tuning knobs (process-wide): blocks_per_sm, bfs_alpha (0: top-down
- * only), bfs_beta, bfs_bitmap, hub_degree, sssp_delta, sssp_delta_scale,
+ * only), bfs_beta, bfs_bitmap, bfs_bu_claim, hub_degree, sssp_delta, sssp_delta_scale,
  * sssp_heavy_split, sssp_item_edges, sssp_warp_degree, sssp_window_scale,
  * sssp_window_degree, sssp_merge_below, sssp_spin_ns, sssp_pair_slices,
  * sssp_stage_flags, sssp_chunk, sssp_item_group, sssp_static_pct, sssp_tail_split,

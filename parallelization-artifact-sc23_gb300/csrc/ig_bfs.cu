@@ -50,11 +50,16 @@ struct BfsArgs {
   // when set, the source is read from the device: the vertex encoded in the
   // low word of *src_key as 0xffffffff - id (connected components' seed)
   const unsigned long long* src_key;
+  // bottom-up levels: 0 = every warp scans its fixed share of 32-vertex
+  // chunks (grid stride); g > 0 = after a first group by warp index, warps
+  // take groups of g chunks from a per-level counter, each claimed while the
+  // previous group is scanned, so the level's end is even
+  int bu_claim;
 };
 
 // Hot counters of the control block, slot s = level % 3: hot32(s) size of the
 // queue built during the level, hot32(3 + s) its hub count, hot64(6 + s) the
-// sum of degrees of the queued vertices.
+// sum of degrees of the queued vertices, hot32(9 + s) bottom-up groups claimed.
 
 __global__ void __launch_bounds__(kThreads) bfs_persistent(BfsArgs a_in) {
   BfsArgs a = a_in;
@@ -105,6 +110,7 @@ __global__ void __launch_bounds__(kThreads) bfs_persistent(BfsArgs a_in) {
       *hot32(ctl, ns) = 0;
       *hot32(ctl, 3 + ns) = 0;
       *hot64(ctl, 6 + ns) = 0;
+      *hot32(ctl, 9 + ns) = 0;
     }
     int* qsize = hot32(ctl, slot);
     int* nhub = hot32(ctl, 3 + slot);
@@ -153,7 +159,8 @@ __global__ void __launch_bounds__(kThreads) bfs_persistent(BfsArgs a_in) {
         if (!grid_sync(ctl, a.timeout_ns, gb)) return;
       }
     } else {
-      for (long long base = gtid & ~31LL; base < a.nodes; base += gthreads) {
+      // one 32-vertex chunk starting at `base` (a multiple of 32)
+      auto scan_chunk = [&](long long base) {
         const long long v = base + lane;
         bool found = false;
         long long deg = 0;
@@ -186,6 +193,20 @@ __global__ void __launch_bounds__(kThreads) bfs_persistent(BfsArgs a_in) {
           if (lane == 0 && (base >> 5) < nwords) nbits[base >> 5] = m;
         }
         warp_append_w(found, (int)v, deg, nxt, qsize, fedges, a.nodes, ctl);
+      };
+      if (a.bu_claim <= 0) {
+        for (long long base = gtid & ~31LL; base < a.nodes; base += gthreads) scan_chunk(base);
+      } else {
+        const long long nchunks = ((long long)a.nodes + 31) >> 5;
+        const long long G = a.bu_claim;
+        int* bgrab = hot32(ctl, 9 + slot);
+        long long q = warp_g;  // group index: chunks [q * G, q * G + G)
+        while (q * G < nchunks) {
+          int ahead = 0;
+          if (lane == 0) ahead = atomicAdd(bgrab, 1);
+          for (long long c = q * G; c < min(q * G + G, nchunks); c++) scan_chunk(c << 5);
+          q = nwarps + (long long)__shfl_sync(IG_FULL, ahead, 0);
+        }
       }
       if (!grid_sync(ctl, a.timeout_ns, gb)) return;
     }
@@ -222,7 +243,7 @@ int igk_bfs(IgExec* ex, const ig_csr* dg, int src, int* d_dist) {
   const IgOptions& o = ig_exec_options(ex);
   BfsArgs a{dg->nindex, dg->nlist, dg->nodes, dg->edges, src, d_dist, (int*)qa, (int*)qb, (int*)hubs,
             ex->d_ctl, ex->timeout_ns, o.hub_degree, o.bfs_alpha, o.bfs_beta, nullptr, 0,
-            o.bfs_bitmap ? (unsigned*)bits : nullptr, nullptr};
+            o.bfs_bitmap ? (unsigned*)bits : nullptr, nullptr, o.bfs_bu_claim};
   void* args[] = {&a};
   return ig_launch_coop(ex, (const void*)bfs_persistent, kThreads, 0, o.blocks_per_sm, args, nullptr);
 }
@@ -242,7 +263,7 @@ int igk_bfs_keyed(IgExec* ex, const ig_csr* dg, const unsigned long long* d_src_
   const IgOptions& o = ig_exec_options(ex);
   BfsArgs a{dg->nindex, dg->nlist, dg->nodes, dg->edges, src, d_dist, (int*)qa, (int*)qb, (int*)hubs,
             ex->d_ctl, ex->timeout_ns, o.hub_degree, o.bfs_alpha, o.bfs_beta, nullptr, 0,
-            o.bfs_bitmap ? (unsigned*)bits : nullptr, d_src_key};
+            o.bfs_bitmap ? (unsigned*)bits : nullptr, d_src_key, o.bfs_bu_claim};
   void* args[] = {&a};
   return ig_launch_coop(ex, (const void*)bfs_persistent, kThreads, 0, o.blocks_per_sm, args, nullptr);
 }
@@ -262,7 +283,7 @@ int igk_bfs_multi(IgExec* ex, const ig_csr* dg, const int* d_sources, int nsourc
   const IgOptions& o = ig_exec_options(ex);
   BfsArgs a{dg->nindex, dg->nlist, dg->nodes, dg->edges, 0, d_dist, (int*)qa, (int*)qb, (int*)hubs,
             ex->d_ctl, ex->timeout_ns, o.hub_degree, o.bfs_alpha, o.bfs_beta, d_sources, nsources,
-            o.bfs_bitmap ? (unsigned*)bits : nullptr, nullptr};
+            o.bfs_bitmap ? (unsigned*)bits : nullptr, nullptr, o.bfs_bu_claim};
   void* args[] = {&a};
   return ig_launch_coop(ex, (const void*)bfs_persistent, kThreads, 0, o.blocks_per_sm, args, nullptr);
 }

@@ -6,6 +6,7 @@ struct IgOptions {
   int bfs_alpha;          // top-down -> bottom-up switch: frontier edges > unexplored / alpha (0: never)
   int bfs_beta;           // bottom-up -> top-down switch: frontier vertices < V / beta
   int bfs_bitmap;         // 1: bottom-up levels test level bitmaps instead of neighbour distances
+  int bfs_bu_claim;       // bottom-up levels: 32-vertex chunks per group claimed from a counter (0: grid stride)
   int hub_degree;         // degree above which a vertex is expanded by the whole grid
   long long sssp_delta;   // near/far bucket width (0 = derived from sampled weights)
   int sssp_delta_scale;   // derived width = mean weight * scale / mean degree

@@ -654,6 +654,7 @@ IgOptions& ig_options() {
       /*bfs_alpha=*/14,
       /*bfs_beta=*/24,
       /*bfs_bitmap=*/1,
+      /*bfs_bu_claim=*/0,
       /*hub_degree=*/256,
       /*sssp_delta=*/0,
       /*sssp_delta_scale=*/128,
@@ -698,7 +699,7 @@ struct OptField {
   {#field, lo, hi, [](IgOptions& o, long long v) { o.field = (decltype(o.field))v; }, \
    [](const IgOptions& o) { return (long long)o.field; }}
 static const OptField g_opt_fields[] = {
-    IG_OPT(blocks_per_sm, 0, 32),     IG_OPT(bfs_alpha, 0, 1000000),   IG_OPT(bfs_beta, 1, 1000000), IG_OPT(bfs_bitmap, 0, 1),
+    IG_OPT(blocks_per_sm, 0, 32),     IG_OPT(bfs_alpha, 0, 1000000),   IG_OPT(bfs_beta, 1, 1000000), IG_OPT(bfs_bitmap, 0, 1), IG_OPT(bfs_bu_claim, 0, 64),
     IG_OPT(hub_degree, 32, INT_MAX),  IG_OPT(sssp_delta, 0, INT_MAX),  IG_OPT(sssp_delta_scale, 1, 1 << 20),
     IG_OPT(sssp_heavy_split, 0, 1),   IG_OPT(sssp_item_edges, 32, 4096), IG_OPT(sssp_warp_degree, 1, INT_MAX),
     IG_OPT(sssp_window_scale, 0, 1 << 20), IG_OPT(sssp_window_degree, 0, INT_MAX),

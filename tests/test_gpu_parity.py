@@ -556,3 +556,26 @@ def test_pagerank_schedule_independent(ig, orc, graphs):
             assert np.abs(outs[0][1] - ref).sum() / ref.sum() <= PR_TOL, name
     finally:
         ig.set_option("pr_static_pct", old)
+
+
+@pytest.mark.parametrize("claim", [1, 4, 16])
+def test_bfs_bottom_up_claims(ig, orc, graphs, claim):
+    """Bottom-up levels whose 32-vertex chunks are taken in groups from a
+    counter instead of a grid stride: exact levels, bottom-up from the
+    first level on (alpha 1) and with the default switch, bitmaps or not."""
+    old = {k: ig.get_option(k) for k in ("bfs_bu_claim", "bfs_alpha", "bfs_bitmap")}
+    try:
+        ig.set_option("bfs_bu_claim", claim)
+        for alpha in (1, 14):
+            ig.set_option("bfs_alpha", alpha)
+            for bitmap in (1, 0):
+                ig.set_option("bfs_bitmap", bitmap)
+                for name in ("rmat14", "hubby", "road128", "two_grids", "star", "rmat18"):
+                    g = graphs[name]
+                    r = run_all(ig, g, [0, g.nodes // 2])
+                    for k, s in enumerate([0, g.nodes // 2]):
+                        assert np.array_equal(r[f"bfs{k}"], orc.bfs(g, s)), (name, s, alpha, bitmap)
+                    assert np.array_equal(r["cc"], orc.cc(g)), name
+    finally:
+        for k, v in old.items():
+            ig.set_option(k, v)
