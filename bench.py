@@ -486,16 +486,16 @@ def load_peaks() -> dict:
 
 
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per call of each
-# algorithm's main kernel on this workload: one ncu capture of that kernel
-# alone (-k, -c 2) on the RMAT scale-21 case (`bench.py --case <algo> --scale
-# 21`: 63,539,260 edges), scaled to RMAT-22 by the edge ratio 2.019 (the
-# traffic grows with the edges processed).  Kernels: sssp_persistent,
-# pr_persistent (15 iterations), tc_count_block (exact and hashed forms; the
-# orientation kernels are not included), bfs_persistent, mis_persistent.
-# The capture and its figures are in the per-kernel traffic summary under
-# profiles/.
-DRAM_BYTES_PER_CALL = {"sssp": 2497888874, "pr": 9041198075, "tc": 3688275862, "bfs": 155368847,
-                       "mis": 167385116}
+# algorithm's kernels on this workload: one ncu capture per algorithm on the
+# RMAT scale-21 case (`bench.py --case <algo> --scale 21`: 63,539,260 edges),
+# scaled to RMAT-22 by the edge ratio 2.019 (the traffic grows with the edges
+# processed).  Kernels: sssp_persistent, pr_persistent (15 iterations),
+# tc_count_block and tc_count_warp (the orientation kernels are not
+# included), bfs_persistent, mis_persistent, and every kernel of the CC call
+# (its seed, its BFS and the union-find kernels).  The capture and its
+# figures are in the per-kernel traffic summary under profiles/.
+DRAM_BYTES_PER_CALL = {"sssp": 2504386466, "pr": 9044022181, "tc": 4027192374, "bfs": 155065402,
+                       "mis": 178654042, "cc": 229072574}
 
 
 # ----------------------------------------------------------------------------- CPU

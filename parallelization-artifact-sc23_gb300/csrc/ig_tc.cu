@@ -347,38 +347,23 @@ __device__ __forceinline__ unsigned long long probe_group(const int* __restrict_
     return contains(out_list + vb, vd, w) ? 1 : 0;
   };
   // lists of at least warp_list probes: the whole warp walks one list at a
-  // time (no per-slot owner search), 128 probes per step while more than 96
-  // remain, then one step of 64 and one of 32 for the rest
+  // time (no per-slot owner search), 128 probes per step with no bounds
+  // tests while 128 remain, then 32 per step for the rest
   unsigned longs = __ballot_sync(IG_FULL, ud >= warp_list);
   while (longs) {
     const int l = __ffs(longs) - 1;
     longs &= longs - 1;
     const int lb = __shfl_sync(IG_FULL, ub, l), le = lb + __shfl_sync(IG_FULL, ud, l);
     int base = lb;
-    for (; le - base > 96; base += 128) {
+    for (; le - base >= 128; base += 128) {
       int w[4];
 #pragma unroll
-      for (int k = 0; k < 4; k++) {
-        const int e = base + k * 32 + lane;
-        w[k] = e < le ? __ldg(&out_list[e]) : -1;
-      }
+      for (int k = 0; k < 4; k++) w[k] = __ldg(&out_list[base + k * 32 + lane]);
 #pragma unroll
-      for (int k = 0; k < 4; k++)
-        if (w[k] >= 0) hits += probe(w[k]);
+      for (int k = 0; k < 4; k++) hits += probe(w[k]);
     }
-    if (le - base > 32) {
-      int w[2];
-#pragma unroll
-      for (int k = 0; k < 2; k++) {
-        const int e = base + k * 32 + lane;
-        w[k] = e < le ? __ldg(&out_list[e]) : -1;
-      }
-#pragma unroll
-      for (int k = 0; k < 2; k++)
-        if (w[k] >= 0) hits += probe(w[k]);
-      base += 64;
-    }
-    if (base + lane < le) hits += probe(__ldg(&out_list[base + lane]));
+    for (; base < le; base += 32)
+      if (base + lane < le) hits += probe(__ldg(&out_list[base + lane]));
   }
   if (ud >= warp_list) ud = 0;
   // short lists: four 32-probe slots per step, load-balanced over the lanes
