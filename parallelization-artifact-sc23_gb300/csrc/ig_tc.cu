@@ -47,7 +47,7 @@ constexpr int kHashCap = 2048;    // block table slots (out-degree <= 1024 is ha
 constexpr int kBitWords = 256;    // block filter: 8192 bits, bit (w mod 8192) set for w in N+(v)
 constexpr int kWarpCap = 256;     // warp table slots (out-degree <= kWarpOut)
 constexpr int kWarpBitWords = 64; // warp filter: 2048 bits
-constexpr int kSpanWords = 4096;  // block bitmap: 131072 bits, bit (w - v - 1) set for w in N+(v)
+constexpr int kSpanWords = 4096;  // block bitmap: 131072 bits over the 32-id words from v + 1's up
 static_assert(kSpanWords >= kHashCap + kBitWords, "the bitmap shares its memory with the table and filter");
 
 // Work items of middle vertex v with `out` out-neighbours and `in`
@@ -63,7 +63,11 @@ __device__ __forceinline__ void tc_items(int out, int in, bool exact, int block_
   *warp_items = (out > 0 && !block) ? (in + kChunk - 1) / kChunk : 0;
   *block_items = block ? (in + block_chunk - 1) / block_chunk : 0;
 }
-__device__ __forceinline__ bool tc_exact(bool ranked, int n, int v) { return ranked && n - 1 - v <= kSpanWords * 32; }
+// Words of the exact bitmap of middle vertex v: word k holds ids
+// [32 (k + wb), 32 (k + wb + 1)) for wb = (v + 1) / 32, so the ids above v
+// need the words up to that of id n - 1.
+__device__ __forceinline__ int tc_span_words(int n, int v) { return v + 1 < n ? ((n - 1) >> 5) - ((v + 1) >> 5) + 1 : 0; }
+__device__ __forceinline__ bool tc_exact(bool ranked, int n, int v) { return ranked && tc_span_words(n, v) <= kSpanWords; }
 
 __device__ __forceinline__ bool before(int du, int u, int dw, int w) { return du < dw || (du == dw && u < w); }
 
@@ -329,10 +333,15 @@ __device__ __forceinline__ unsigned long long probe_group(const int* __restrict_
   }
   // membership of w in N+(v): filter bit first (rejects most misses with one
   // shared load), then the hash table or a binary search of N+(v)
+  // exact bitmap: the word of id w is at the shared address sh0 + 4 (w / 32)
+  // (sh0 folds the bitmap's first word in), so a probe is a shift, one
+  // shared load and a bit test (w > v: only the part of N+(u) after v is scanned)
+  const unsigned sh0 = kExact ? (unsigned)__cvta_generic_to_shared(bits) - 4u * (unsigned)((v + 1) >> 5) : 0u;
   auto probe = [&](int w) -> int {
     if (kExact) {
-      const unsigned x = (unsigned)(w - v - 1);  // w > v: only the part of N+(u) after v is scanned
-      return (bits[x >> 5] >> (x & 31)) & 1u;
+      unsigned word;
+      asm volatile("ld.shared.u32 %0, [%1];" : "=r"(word) : "r"(sh0 + ((unsigned)(w >> 5) << 2)));
+      return (word >> (w & 31)) & 1u;
     }
     if (hashed) {
       if (((bits[(w >> 5) & (kBits - 1)] >> (w & 31)) & 1u) == 0) return 0;
@@ -512,8 +521,7 @@ __global__ void __launch_bounds__(kThreads, 8) tc_count_block(const int* __restr
   for (int run = next_run(-1); run < items; run = next_run(run))
   for (int it = run; it < (grab > 0 ? min(run + grab, items) : run + 1); it++) {
     const int v = __ldg(&item_v[it]);  // middle vertex (block-uniform)
-    const int span = n - 1 - v;        // ids above v
-    if ((ranked && span <= kSpanWords * 32) != kExact) continue;  // the other launch's item
+    if (tc_exact(ranked, n, v) != kExact) continue;  // the other launch's item
     const int vb = __ldg(&out_off[v]);
     const int vd = __ldg(&out_off[v + 1]) - vb;
     __syncthreads();  // the previous item's probes are done with the table and the counter
@@ -521,12 +529,13 @@ __global__ void __launch_bounds__(kThreads, 8) tc_count_block(const int* __restr
       cur_v = v;
       hashed = !kExact && 2 * vd <= kHashCap;
       if (kExact) {
-        const int words = (span + 31) >> 5;
+        const int words = tc_span_words(n, v);
+        const int wb = (v + 1) >> 5;
         for (int k = threadIdx.x; k < words; k += blockDim.x) s_mem[k] = 0u;
         __syncthreads();
         for (int k = threadIdx.x; k < vd; k += blockDim.x) {
-          const unsigned x = (unsigned)(__ldg(&out_list[vb + k]) - v - 1);
-          atomicOr(&s_mem[x >> 5], 1u << (x & 31));
+          const int w = __ldg(&out_list[vb + k]);
+          atomicOr(&s_mem[(w >> 5) - wb], 1u << (w & 31));
         }
       } else if (hashed) {
         int cap = 32;
