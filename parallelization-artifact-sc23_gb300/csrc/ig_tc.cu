@@ -202,7 +202,9 @@ __global__ void __launch_bounds__(kThreads) tc_orient_fill(const int* __restrict
 }
 
 // Vertices above kOrientHub neighbours, one block each: count (and check)
-// their out-neighbours.
+// their out-neighbours.  With ids in (degree, id) order a hub's out part is
+// the suffix above it, found by one thread with a binary search (the fill
+// checks the list).
 __global__ void __launch_bounds__(kThreads) tc_orient_hubs_count(const int* __restrict__ nindex,
                                                                  const int* __restrict__ nlist, int n,
                                                                  const int* hubs, int* out_cnt, int* item_cnt,
@@ -211,6 +213,23 @@ __global__ void __launch_bounds__(kThreads) tc_orient_hubs_count(const int* __re
   __shared__ int s_tmp[33];
   const int nh = ctl->i32[0];
   const bool ranked = ctl->i32[1] == 0;
+  if (ranked) {
+    for (long long h = (long long)blockIdx.x * blockDim.x + threadIdx.x; h < nh;
+         h += (long long)gridDim.x * blockDim.x) {
+      const int u = hubs[h];
+      const int b = __ldg(&nindex[u]), e = __ldg(&nindex[u + 1]);
+      int lo = b, hi = e;  // first entry above u
+      while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        if (__ldg(&nlist[mid]) <= u) lo = mid + 1;
+        else hi = mid;
+      }
+      const int total = e - lo;
+      out_cnt[u] = total;
+      tc_items(total, e - b - total, tc_exact(true, n, u), block_chunk, &item_cnt[u], &item_cnt_b[u]);
+    }
+    return;
+  }
   for (int h = blockIdx.x; h < nh; h += gridDim.x) {
     const int u = hubs[h];
     const int b = __ldg(&nindex[u]), e = __ldg(&nindex[u + 1]), du = e - b;
@@ -232,30 +251,60 @@ __global__ void __launch_bounds__(kThreads) tc_orient_hubs_count(const int* __re
   }
 }
 
-// Order-preserving split of the hub lists into out and in parts, one block per hub.
+// Order-preserving split of the hub lists into out and in parts, one block
+// per hub.  With ids in (degree, id) order the hubs are the last nh ids and
+// their lists one contiguous range of nlist, copied in 256-entry chunks
+// spread over all blocks (a chunk spans at most two hub lists, each longer
+// than kOrientHub), each entry checked (sorted, no self loop, in range).
 __global__ void __launch_bounds__(kThreads) tc_orient_hubs_fill(const int* __restrict__ nindex,
-                                                                const int* __restrict__ nlist, const int* hubs,
+                                                                const int* __restrict__ nlist, int n,
+                                                                const int* hubs,
                                                                 const int* __restrict__ out_off, int* out_list,
-                                                                int* in_list, const IgCtl* ctl) {
+                                                                int* in_list, IgCtl* ctl) {
   using namespace ig;
   __shared__ int s_tmp[33];
+  __shared__ int s_u0;
   if (ctl->err) return;
   const int nh = ctl->i32[0];
   const bool ranked = ctl->i32[1] == 0;
+  static_assert(kThreads <= kOrientHub, "a chunk must span at most two hub lists");
+  if (ranked) {
+    if (nh == 0) return;
+    const int h0 = n - nh;  // first hub id
+    const long long k0 = __ldg(&nindex[h0]), k1 = __ldg(&nindex[n]);
+    bool bad = false;
+    for (long long c0 = k0 + (long long)blockIdx.x * blockDim.x; c0 < k1; c0 += (long long)gridDim.x * blockDim.x) {
+      __syncthreads();
+      if (threadIdx.x == 0) {  // hub holding entry c0: last u in [h0, n) with nindex[u] <= c0
+        int lo = h0, hi = n - 1;
+        while (lo < hi) {
+          const int mid = (lo + hi + 1) >> 1;
+          if (__ldg(&nindex[mid]) <= c0) lo = mid;
+          else hi = mid - 1;
+        }
+        s_u0 = lo;
+      }
+      __syncthreads();
+      const long long k = c0 + threadIdx.x;
+      if (k < k1) {
+        const int u0 = s_u0;
+        const int u = (u0 + 1 < n && k >= __ldg(&nindex[u0 + 1])) ? u0 + 1 : u0;
+        const int b = __ldg(&nindex[u]), e = __ldg(&nindex[u + 1]);
+        const int op = out_off[u];
+        const int split = e - (out_off[u + 1] - op);
+        const int w = __ldg(&nlist[k]);
+        if (w == u || (k > b && __ldg(&nlist[k - 1]) >= w) || w < 0 || w >= n) bad = true;
+        else if (k >= split) out_list[op + (k - split)] = w;
+        else in_list[(b - op) + (k - b)] = w;
+      }
+    }
+    if (bad) raise(ctl, IG_ERR_UNSORTED);
+    return;
+  }
   for (int h = blockIdx.x; h < nh; h += gridDim.x) {
     const int u = hubs[h];
     const int b = __ldg(&nindex[u]), e = __ldg(&nindex[u + 1]), du = e - b;
     int op = out_off[u], ip = b - op;
-    if (ranked) {
-      // (degree, id) order: in part = the prefix below u, out part = the suffix
-      const int split = e - (out_off[u + 1] - op);
-      for (int k = b + threadIdx.x; k < e; k += blockDim.x) {
-        const int w = __ldg(&nlist[k]);
-        if (k >= split) out_list[op + (k - split)] = w;
-        else in_list[ip + (k - b)] = w;
-      }
-      continue;
-    }
     for (int t = b; t < e; t += blockDim.x) {
       const int k = t + threadIdx.x;
       int w = 0;
@@ -642,7 +691,7 @@ static int tc_run(IgExec* ex, int nodes, int edges, const int* d_nindex, const i
   if ((rc = igk_exclusive_scan(ex, (const int*)icnt_b, (int*)ioff_b, nodes, nullptr))) return rc;
   tc_orient_fill<<<grid, kThreads, 0, ex->stream>>>(d_nindex, d_nlist, nodes, (const int*)off, (int*)list,
                                                      (int*)inl, ex->d_ctl);
-  tc_orient_hubs_fill<<<ex->sms * 8, kThreads, 0, ex->stream>>>(d_nindex, d_nlist, (const int*)hubs,
+  tc_orient_hubs_fill<<<ex->sms * 8, kThreads, 0, ex->stream>>>(d_nindex, d_nlist, nodes, (const int*)hubs,
                                                                 (const int*)off, (int*)list, (int*)inl, ex->d_ctl);
   tc_item_owner<<<grid, kThreads, 0, ex->stream>>>((const int*)ioff, nodes, (int*)itemv);
   tc_item_owner<<<grid, kThreads, 0, ex->stream>>>((const int*)ioff_b, nodes, (int*)itemv_b);

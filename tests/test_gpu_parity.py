@@ -305,6 +305,27 @@ def test_tc_rejects_unsorted(ig, graphs):
         assert dist[0] == 0
 
 
+@pytest.mark.parametrize("where", ["hub", "light"])
+def test_tc_rejects_unsorted_ranked(ig, orc, graphs, where):
+    """Ids in (degree, id) order: a swapped pair in a hub's list (checked by
+    the chunked hub copy) or in a short list (checked by the count pass) is
+    reported as unsorted; the sorted input counts right."""
+    g = graphs["rmat18"].degree_ordered()
+    deg = np.diff(g.nindex)
+    with ig.DeviceCSR(g) as d:
+        assert ig.GPUtc_vertex(g.nodes, d.nindex_ptr, d.nlist_ptr)[0] == orc.tc(g)
+    v = int(np.argmax(deg)) if where == "hub" else int(np.argmax((deg > 2) & (deg < 64)))
+    assert (deg[v] > 256) == (where == "hub")
+    nl = g.nlist.copy()
+    b = int(g.nindex[v]) + int(deg[v]) // 2
+    nl[b], nl[b + 1] = nl[b + 1], nl[b]
+    bad = ig.Graph(g.nindex, nl)
+    with ig.DeviceCSR(bad) as d:
+        with pytest.raises(ig.IndigoError) as e:
+            ig.GPUtc_vertex(bad.nodes, d.nindex_ptr, d.nlist_ptr)
+        assert e.value.status == ig._lib.IG_ERR_UNSORTED
+
+
 def test_bounded_wait_reports_timeout(ig, graphs):
     """A grid barrier that one block never reaches ends in IG_ERR_TIMEOUT
     after the bound, and the device keeps working afterwards."""
