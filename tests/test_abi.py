@@ -54,15 +54,20 @@ def test_options_roundtrip(ig):
 
 
 def test_kernel_option_defaults_and_ranges(ig):
-    """The SSSP work-item and degree-window knobs and the PageRank residency
-    have the measured defaults, accept their range and refuse values outside
-    it (the work-item size is capped so a round's slice count stays small)."""
-    defaults = {"sssp_item_edges": 256, "sssp_warp_degree": 64, "sssp_window_scale": 8,
-                "sssp_window_degree": 16, "pr_blocks_per_sm": 4, "tc_block_chunk": 4096}
+    """The scheduling and work-split knobs have the measured defaults, accept
+    their range and refuse values outside it (the work-item size is capped
+    so a round's slice count stays small; shares are percentages)."""
+    defaults = {"sssp_item_edges": 128, "sssp_warp_degree": 64, "sssp_window_scale": 8,
+                "sssp_window_degree": 16, "sssp_stage_flags": 1, "sssp_static_pct": 75,
+                "sssp_chunk": 32, "sssp_item_group": 8, "sssp_tail_split": 1, "sssp_claim_ahead": 0,
+                "mis_static_pct": 0, "pr_blocks_per_sm": 4, "pr_static_pct": 0, "tc_block_chunk": 4096,
+                "tc_grab": 2, "tc_warp_list": 64, "bfs_bu_claim": 0, "cc_bfs_seed": 1}
     for name, value in defaults.items():
         assert ig.get_option(name) == value, name
     for name, ok, bad in [("sssp_item_edges", 4096, 4097), ("sssp_item_edges", 32, 31),
-                          ("sssp_window_scale", 0, -1), ("sssp_window_degree", 0, -1)]:
+                          ("sssp_window_scale", 0, -1), ("sssp_window_degree", 0, -1),
+                          ("sssp_static_pct", 100, 101), ("pr_static_pct", 0, -1), ("sssp_chunk", 32, 33),
+                          ("sssp_item_group", 1, 0), ("tc_warp_list", 1, 0), ("bfs_bu_claim", 64, 65)]:
         old = ig.get_option(name)
         try:
             ig.set_option(name, ok)
