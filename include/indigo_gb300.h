@@ -151,7 +151,7 @@ int ig_set_wait_timeout_ms(int ms);
  * sssp_static_pct, sssp_tail_split, sssp_claim_ahead, sssp_expanded_check,
  * mis_static_pct, pr_hub_degree, pr_chunk, pr_blocks_per_sm, pr_prefetch,
  * pr_subwarp, pr_static_pct, pr_two_pass, tc_block_chunk, tc_grab,
- * tc_warp_list, cc_bfs_seed, cc_rounds.  Every setting gives the same
+ * tc_warp_list, tc_runs, cc_bfs_seed, cc_rounds.  Every setting gives the same
  * results; they trade speed. */
 int ig_set_option(const char* name, long long value);
 int ig_get_option(const char* name, long long* value);

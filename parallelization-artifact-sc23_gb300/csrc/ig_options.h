@@ -29,6 +29,7 @@ struct IgOptions {
                           // (no atomics); the rest are taken from a counter
   int sssp_tail_split;    // SSSP: chunks / slice groups taken from the counter are this many times smaller
   int sssp_claim_ahead;   // SSSP: 1 = a warp claims its next chunk from the counter as it starts the current
+  int sssp_expanded_check;// SSSP: 1 = skip a queued vertex whose distance has not dropped since it was expanded
   int mis_static_pct;     // MIS: percent of a round's worklist groups dealt round-robin (no atomics)
   int pr_hub_degree;      // PageRank: degree above which a vertex is split in chunks
   int pr_chunk;           // PageRank: edges per hub chunk
@@ -43,6 +44,8 @@ struct IgOptions {
                           // vertex's items mostly share one block and its table (0: grid stride)
   int tc_warp_list;       // TC: probe lists at least this long are walked by the whole warp, shorter ones
                           // share the warp's slots through an owner search
+  int tc_runs;            // TC: 1 = short probe lists expanded four consecutive slots per lane (one owner
+                          // search per lane and step), 0 = an owner search per slot
   int cc_bfs_seed;        // CC: 1 = the largest-degree vertex's component labelled by a BFS from it,
                           // union-find for the rest (0 = neighbour sampling, then union-find;
                           // cc_rounds chooses the sampling form)

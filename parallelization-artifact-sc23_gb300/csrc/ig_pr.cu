@@ -400,11 +400,15 @@ __global__ void __launch_bounds__(kThreads, 4) pr_persistent(PrArgs a) {
       if (lane == 0) a.partial[c] = make_float2(shi, slo);
     }
     // Vertex groups: this warp's sequence is warp_g, warp_g + nwarps, ...
-    // below nstatic, then groups claimed from the counter.  Each lane's list
-    // range of the warp's next group is loaded (and its list prefetched into
-    // L2), and the group after it claimed, while the current group is summed.
+    // below nstatic, then units of `unit` consecutive groups claimed from the
+    // counter (a unit of one group unless the graph has more than 32 groups
+    // per warp, as a batched pack does, so the counter takes about 32 claims
+    // per warp).  Each lane's list range of the warp's next group is loaded
+    // (and its list prefetched into L2), and the unit after it claimed, while
+    // the current group is summed.
     const long long ngroups = ((long long)a.nodes + 31) >> 5;
     const long long nstatic = max(min(ngroups, (long long)nwarps), ngroups * a.static_pct / 100);
+    const long long unit = max(1LL, (ngroups - nstatic) / (32LL * nwarps));
     auto load_ranges = [&](long long grp, int& rb, int& re) {
       const long long vn = grp * 32 + lane;
       rb = re = 0;
@@ -414,13 +418,16 @@ __global__ void __launch_bounds__(kThreads, 4) pr_persistent(PrArgs a) {
         if (a.prefetch && re - rb <= a.hub_degree) prefetch_list(a, kTwo ? (const void*)a.vals : a.nlist, rb, re);
       }
     };
-    long long grp = warp_g, gnext;
+    // first group of claimed unit c, and the end of the unit
+    auto unit_first = [&](unsigned long long c) { return nstatic + (long long)c * unit; };
+    long long grp = warp_g, gnext, uend = 0;  // uend: end of the claimed unit that holds gnext
     if (grp + nwarps < nstatic) {
       gnext = grp + nwarps;
     } else {
       unsigned long long c = 0;
-      if (lane == 0) c = (unsigned long long)nstatic + atomicAdd(grab, 1ull);
-      gnext = (long long)__shfl_sync(IG_FULL, c, 0);
+      if (lane == 0) c = atomicAdd(grab, 1ull);
+      gnext = unit_first(__shfl_sync(IG_FULL, c, 0));
+      uend = min(gnext + unit, ngroups);
     }
     int nb = 0, ne = 0;
     load_ranges(grp, nb, ne);
@@ -428,10 +435,12 @@ __global__ void __launch_bounds__(kThreads, 4) pr_persistent(PrArgs a) {
       const long long vi = grp * 32 + lane;
       int v = (int)vi;
       const int b = nb, e = ne;
-      // the group after gnext: static, or claimed now (used at the end)
-      const bool claim = gnext < ngroups && gnext + nwarps >= nstatic;
+      // the group after gnext: the next static one, the next in its unit,
+      // or the first of a unit claimed now (used at the end)
+      const bool dyn = gnext >= nstatic;
+      const bool claim = gnext < ngroups && (dyn ? gnext + 1 >= uend : gnext + nwarps >= nstatic);
       unsigned long long claimed = 0;
-      if (claim && lane == 0) claimed = (unsigned long long)nstatic + atomicAdd(grab, 1ull);
+      if (claim && lane == 0) claimed = atomicAdd(grab, 1ull);
       load_ranges(gnext, nb, ne);
       int d = e - b;
       float sum = 0.f;
@@ -513,7 +522,12 @@ __global__ void __launch_bounds__(kThreads, 4) pr_persistent(PrArgs a) {
       }
       if (kBatched) warp_add_by_graph(gcur, vg, verr, upd);
       grp = gnext;
-      gnext = claim ? (long long)__shfl_sync(IG_FULL, claimed, 0) : gnext + nwarps;
+      if (claim) {
+        gnext = unit_first(__shfl_sync(IG_FULL, claimed, 0));
+        uend = min(gnext + unit, ngroups);
+      } else {
+        gnext = dyn ? gnext + 1 : gnext + nwarps;
+      }
     }
     // ---- phase B: combine hub chunks in chunk order
     if (nh > 0) {

@@ -18,10 +18,11 @@
 // long list and one grid barrier ends each round.  An
 // improved vertex with distance < T joins the next near queue
 // (once per iteration, by stamp) and otherwise the far pile (once per epoch,
-// by flag).  A queued vertex is expanded only if its distance is below the
-// one it was last expanded with (re-queued vertices are often expanded
-// already).  A vertex of degree d above window_degree is expanded only once
-// its distance is below m + C / d (m: the smallest distance queued for the
+// by flag).  With expanded_check, a queued vertex is expanded only if its
+// distance is below the one it was last expanded with (off by default: it
+// skips about 1% of the entries for a random read and write per entry).
+// A vertex of degree d above window_degree is expanded only once its
+// distance is below m + C / d (m: the smallest distance queued for the
 // round, C: the window constant) and is otherwise queued again for the next
 // round: a list is expensive to expand with a distance that later improves,
 // so the longer the list, the closer to Dijkstra order it is expanded, while
@@ -87,6 +88,8 @@ struct SsspArgs {
   int static_pct;        // share (percent) of a pass's chunks / slice groups dealt to warps without atomics
   int tail_split;        // chunks / slice groups taken from the counter are this many times smaller
   int claim_ahead;       // 1: a warp claims its next chunk from the counter when it starts the current one
+  int expanded_check;    // 1: a queued vertex is skipped when its distance has not dropped since its last
+                         // expansion (one more random read and write per queue entry)
 };
 
 // Per-round counters: hot counters of the control block (every warp updates
@@ -143,7 +146,7 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) sssp_persistent(SsspArgs
     a.dist[v] = (v == a.src) ? 0 : kInf;
     a.stamp[v] = 0;
     a.farflag[v] = 0;
-    a.expanded[v] = kInf;
+    if (a.expanded_check) a.expanded[v] = kInf;
     if (a.heavy_split) a.inmember[v] = 0;  // read only by the light/heavy split
   }
   if (gtid < kDeltaSamples && a.edges > 0) {  // whole warps (kDeltaSamples is a multiple of 32)
@@ -373,7 +376,7 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) sssp_persistent(SsspArgs
           u = frontier[i];
           // every per-vertex read depends only on u, so they are issued together
           du = a.dist[u];
-          const int ex = heavy ? kInf : a.expanded[u];
+          const int ex = (heavy || !a.expanded_check) ? kInf : a.expanded[u];
           beg = __ldg(&a.nindex[u]);
           const int end = __ldg(&a.nindex[u + 1]);
           if (heavy) {
@@ -398,7 +401,7 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) sssp_persistent(SsspArgs
                   defer = a.stamp[u] != next_stamp && atomicExch(&a.stamp[u], next_stamp) != next_stamp;
                 }
               } else {
-                a.expanded[u] = du;
+                if (a.expanded_check) a.expanded[u] = du;
               }
             }
 
@@ -764,7 +767,9 @@ int igk_sssp(IgExec* ex, const ig_csr* dg, int src, int* d_dist) {
                            &smalls)))
     return rc;
   void *expanded, *members, *inmember;
-  if ((rc = ig_scratch_get(ex->scratch, IG_SLOT_F0, vb, &expanded))) return rc;
+  expanded = nullptr;  // only with the expanded-distance check
+  if (ig_exec_options(ex).sssp_expanded_check && (rc = ig_scratch_get(ex->scratch, IG_SLOT_F0, vb, &expanded)))
+    return rc;
   if ((rc = ig_scratch_get(ex->scratch, IG_SLOT_F1, vb, &members))) return rc;
   if ((rc = ig_scratch_get(ex->scratch, IG_SLOT_E0, vb, &inmember))) return rc;
   if ((rc = ig_exec_reset(ex))) return rc;
@@ -776,7 +781,7 @@ int igk_sssp(IgExec* ex, const ig_csr* dg, int src, int* d_dist) {
              (int*)expanded, (int*)members, (int*)inmember, ex->d_ctl, ex->timeout_ns, o.sssp_item_edges,
              o.sssp_warp_degree,
              o.sssp_delta, o.sssp_delta_scale, o.sssp_heavy_split, o.sssp_window_scale,
-             o.sssp_window_degree, o.sssp_merge_below, o.sssp_spin_ns, o.sssp_stage_flags, o.sssp_chunk, o.sssp_item_group, o.sssp_static_pct, o.sssp_tail_split, o.sssp_claim_ahead};
+             o.sssp_window_degree, o.sssp_merge_below, o.sssp_spin_ns, o.sssp_stage_flags, o.sssp_chunk, o.sssp_item_group, o.sssp_static_pct, o.sssp_tail_split, o.sssp_claim_ahead, o.sssp_expanded_check};
   void* args[] = {&a};
   // the register budget follows the residency cap (4, 5 or 6 blocks of 256 threads per SM)
   // (the paired-slice form holds more registers: 3 blocks per SM, or 4 with spills)

@@ -346,6 +346,59 @@ __global__ void __launch_bounds__(kThreads) tc_item_owner(const int* __restrict_
   }
 }
 
+// Expansion of the 32 lanes' lists [beg, beg + deg) in steps of 128 slots,
+// each lane taking four consecutive slots: one owner search per lane and
+// step (five shuffles) for its first slot, then a walk forward over the list
+// ends held in the warp's shared scratch `own` (65 ints), instead of one
+// owner search per slot.  visit4(act[4], edge[4]) is called warp-uniformly.
+template <class Visit4>
+__device__ __forceinline__ void warp_expand_runs4(int beg, int deg, int* own, Visit4&& visit4) {
+  const int lane = ig::lane_id();
+  int incl = deg;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int t = __shfl_up_sync(IG_FULL, incl, o);
+    if (lane >= o) incl += t;
+  }
+  const int total = __shfl_sync(IG_FULL, incl, 31);
+  if (total == 0) return;
+  const int excl = incl - deg;
+  int* s_excl = own;       // [33]: list starts in slot numbering, then the total
+  int* s_beg = own + 33;   // [32]: list starts in the edge array
+  __syncwarp();
+  s_excl[lane] = excl;
+  s_beg[lane] = beg;
+  if (lane == 31) s_excl[32] = total;
+  __syncwarp();
+  for (int base = 0; base < total; base += 128) {
+    const int s0 = base + 4 * lane;
+    int j = 0;  // last list starting at or before s0 (a non-empty one when s0 < total)
+#pragma unroll
+    for (int step = 16; step >= 1; step >>= 1) {
+      const int ex = __shfl_sync(IG_FULL, excl, j + step);
+      if (ex <= s0) j += step;
+    }
+    bool act[4];
+    int e[4];
+    int jn = s_excl[j + 1], jb = s_beg[j] - s_excl[j];
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+      const int sl = s0 + k;
+      act[k] = sl < total;
+      if (act[k]) {
+        while (sl >= jn) {  // ends within the total: list 31 ends at s_excl[32]
+          j++;
+          jn = s_excl[j + 1];
+          jb = s_beg[j] - s_excl[j];
+        }
+      }
+      e[k] = act[k] ? jb + sl : 0;
+    }
+    visit4(act, e);
+  }
+  __syncwarp();
+}
+
 // Probes of one group of <= 32 in-neighbours u of middle vertex v, one per
 // lane (in_list[g .. gend)): every w of N+(u) (only the part after v when ids
 // are in (degree, id) order) is looked up in N+(v): with kExact in the bitmap
@@ -359,7 +412,7 @@ __device__ __forceinline__ unsigned long long probe_group(const int* __restrict_
                                                           const int* __restrict__ in_list, int g, int gend, int v,
                                                           int vb, int vd, bool ranked, const int* tab,
                                                           const unsigned* bits, unsigned mask, bool hashed,
-                                                          int warp_list) {
+                                                          int warp_list, int* own) {
   using namespace ig;
   const int lane = lane_id();
   unsigned hits = 0;  // this lane's, within one group
@@ -424,15 +477,21 @@ __device__ __forceinline__ unsigned long long probe_group(const int* __restrict_
       if (base + lane < le) hits += probe(__ldg(&out_list[base + lane]));
   }
   if (ud >= warp_list) ud = 0;
-  // short lists: four 32-probe slots per step, load-balanced over the lanes
-  warp_expand4(ub, ud, [&](const bool (&act)[4], const int (&e)[4], const int (&)[4]) {
+  // short lists: 128 probe slots per step, load-balanced over the lanes
+  // (four consecutive slots per lane with `own`, else four 32-slot columns,
+  // each with its own owner search)
+  auto visit = [&](const bool (&act)[4], const int (&e)[4]) {
     int w[4];
 #pragma unroll
     for (int k = 0; k < 4; k++) w[k] = act[k] ? __ldg(&out_list[e[k]]) : -1;
 #pragma unroll
     for (int k = 0; k < 4; k++)
       if (act[k]) hits += probe(w[k]);
-  });
+  };
+  if (own)
+    warp_expand_runs4(ub, ud, own, visit);
+  else
+    warp_expand4(ub, ud, [&](const bool (&act)[4], const int (&e)[4], const int (&)[4]) { visit(act, e); });
   return hits;
 }
 
@@ -468,9 +527,10 @@ __global__ void __launch_bounds__(kThreads) tc_count_warp(const int* __restrict_
                                                           const int* __restrict__ item_v, int n,
                                                           unsigned long long* count, const IgCtl* ctl,
                                                           const int* __restrict__ graph_vptr, int graphs,
-                                                          int warp_list) {
+                                                          int warp_list, int runs) {
   using namespace ig;
   __shared__ int s_tab[kWarps][kWarpCap + kWarpBitWords];
+  __shared__ int s_own[kWarps][65];
   if (ctl->err) return;
   const int lane = lane_id(), wib = threadIdx.x >> 5;
   int* tab = s_tab[wib];
@@ -514,7 +574,7 @@ __global__ void __launch_bounds__(kThreads) tc_count_warp(const int* __restrict_
     const unsigned long long before_item = local;
     for (int g = c0; g < c1; g += 32)
       local += probe_group<kWarpBitWords>(out_off, out_list, in_list, g, c1, v, vb, vd, ranked, tab, bits, mask,
-                                          hashed, warp_list);
+                                          hashed, warp_list, runs ? s_own[wib] : nullptr);
     if (kBatched) tc_add_graph(local - before_item, count, graph_vptr, graphs, v);
   }
   if constexpr (!kBatched) {
@@ -541,12 +601,14 @@ __global__ void __launch_bounds__(kThreads, 8) tc_count_block(const int* __restr
                                                               unsigned long long* count, const IgCtl* ctl,
                                                               const int* __restrict__ graph_vptr, int graphs,
                                                               int block_chunk, int grab, int* grab_ctr,
-                                                              int warp_list) {
+                                                              int warp_list, int runs) {
   using namespace ig;
   // the exact bitmap, or the hash table followed by the filter
   __shared__ unsigned s_mem[kExact ? kSpanWords : kHashCap + kBitWords];
   __shared__ int s_next;
   __shared__ int s_run;
+  __shared__ int s_own[kWarps][65];
+  int* own = runs ? s_own[threadIdx.x >> 5] : nullptr;
   int* tab = (int*)s_mem;
   unsigned* bits = s_mem + kHashCap;
   if (ctl->err) return;
@@ -620,10 +682,10 @@ __global__ void __launch_bounds__(kThreads, 8) tc_count_block(const int* __restr
       const int ge = min(g + gsz, c1);
       if constexpr (kExact)
         local += probe_group<kBitWords, true>(out_off, out_list, in_list, g, ge, v, vb, vd, true, tab, s_mem, mask,
-                                              false, warp_list);
+                                              false, warp_list, own);
       else
         local += probe_group<kBitWords>(out_off, out_list, in_list, g, ge, v, vb, vd, ranked, tab, bits, mask,
-                                        hashed, warp_list);
+                                        hashed, warp_list, own);
     }
     if (kBatched) tc_add_graph(local - before_item, count, graph_vptr, graphs, v);
   }
@@ -654,6 +716,7 @@ static int tc_run(IgExec* ex, int nodes, int edges, const int* d_nindex, const i
   const int block_chunk = ig_exec_options(ex).tc_block_chunk;
   const int grab = ig_exec_options(ex).tc_grab;
   const int wl = ig_exec_options(ex).tc_warp_list;
+  const int runs = ig_exec_options(ex).tc_runs;
   void *cnt, *off, *icnt, *ioff, *icnt_b, *ioff_b, *list, *inl, *hubs, *itemv, *itemv_b;
   int rc;
   if ((rc = ig_scratch_get(ex->scratch, IG_SLOT_V0, vb, &cnt))) return rc;
@@ -699,23 +762,23 @@ static int tc_run(IgExec* ex, int nodes, int edges, const int* d_nindex, const i
   if (d_graph_vptr) {
     tc_count_block<true, true><<<cgrid, kThreads, 0, ex->stream>>>(
         (const int*)off, (const int*)list, d_nindex, (const int*)inl, (const int*)ioff_b, (const int*)itemv_b, nodes,
-        d_count, ex->d_ctl, d_graph_vptr, graphs, block_chunk, grab, &ex->d_ctl->hot[0], wl);
+        d_count, ex->d_ctl, d_graph_vptr, graphs, block_chunk, grab, &ex->d_ctl->hot[0], wl, runs);
     tc_count_block<true, false><<<cgrid, kThreads, 0, ex->stream>>>(
         (const int*)off, (const int*)list, d_nindex, (const int*)inl, (const int*)ioff_b, (const int*)itemv_b, nodes,
-        d_count, ex->d_ctl, d_graph_vptr, graphs, block_chunk, grab, &ex->d_ctl->hot[kCtlSpread], wl);
+        d_count, ex->d_ctl, d_graph_vptr, graphs, block_chunk, grab, &ex->d_ctl->hot[kCtlSpread], wl, runs);
     tc_count_warp<true><<<cgrid, kThreads, 0, ex->stream>>>((const int*)off, (const int*)list, d_nindex,
                                                             (const int*)inl, (const int*)ioff, (const int*)itemv,
-                                                            nodes, d_count, ex->d_ctl, d_graph_vptr, graphs, wl);
+                                                            nodes, d_count, ex->d_ctl, d_graph_vptr, graphs, wl, runs);
   } else {
     tc_count_block<false, true><<<cgrid, kThreads, 0, ex->stream>>>(
         (const int*)off, (const int*)list, d_nindex, (const int*)inl, (const int*)ioff_b, (const int*)itemv_b, nodes,
-        d_count, ex->d_ctl, nullptr, 0, block_chunk, grab, &ex->d_ctl->hot[0], wl);
+        d_count, ex->d_ctl, nullptr, 0, block_chunk, grab, &ex->d_ctl->hot[0], wl, runs);
     tc_count_block<false, false><<<cgrid, kThreads, 0, ex->stream>>>(
         (const int*)off, (const int*)list, d_nindex, (const int*)inl, (const int*)ioff_b, (const int*)itemv_b, nodes,
-        d_count, ex->d_ctl, nullptr, 0, block_chunk, grab, &ex->d_ctl->hot[kCtlSpread], wl);
+        d_count, ex->d_ctl, nullptr, 0, block_chunk, grab, &ex->d_ctl->hot[kCtlSpread], wl, runs);
     tc_count_warp<false><<<cgrid, kThreads, 0, ex->stream>>>((const int*)off, (const int*)list, d_nindex,
                                                              (const int*)inl, (const int*)ioff, (const int*)itemv,
-                                                             nodes, d_count, ex->d_ctl, nullptr, 0, wl);
+                                                             nodes, d_count, ex->d_ctl, nullptr, 0, wl, runs);
   }
   ig_count_launches(10);
   return ig_cuda_check((int)cudaGetLastError(), "tc launch");

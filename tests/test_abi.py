@@ -60,6 +60,7 @@ def test_kernel_option_defaults_and_ranges(ig):
     defaults = {"sssp_item_edges": 128, "sssp_warp_degree": 64, "sssp_window_scale": 8,
                 "sssp_window_degree": 16, "sssp_stage_flags": 1, "sssp_static_pct": 75,
                 "sssp_chunk": 32, "sssp_item_group": 8, "sssp_tail_split": 1, "sssp_claim_ahead": 0,
+                "sssp_expanded_check": 0,
                 "mis_static_pct": 0, "pr_blocks_per_sm": 4, "pr_static_pct": 0, "tc_block_chunk": 4096,
                 "tc_grab": 2, "tc_warp_list": 64, "bfs_bu_claim": 0, "cc_bfs_seed": 1}
     for name, value in defaults.items():

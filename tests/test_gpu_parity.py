@@ -600,3 +600,44 @@ def test_bfs_bottom_up_claims(ig, orc, graphs, claim):
     finally:
         for k, v in old.items():
             ig.set_option(k, v)
+
+
+@pytest.mark.parametrize("check", [0, 1])
+def test_sssp_expanded_check_forms(ig, orc, graphs, check):
+    """Queued vertices skipped when their distance has not dropped since
+    their last expansion, or expanded again: exact distances either way
+    (with and without the degree window, most lists as work items or not)."""
+    old = {k: ig.get_option(k) for k in ("sssp_expanded_check", "sssp_window_scale", "sssp_warp_degree")}
+    try:
+        ig.set_option("sssp_expanded_check", check)
+        for ws, wd in ((8, 64), (0, 64), (8, 4)):
+            ig.set_option("sssp_window_scale", ws)
+            ig.set_option("sssp_warp_degree", wd)
+            for name in ("rmat14", "hubby", "road128", "star", "rmat18"):
+                g = graphs[name]
+                with ig.DeviceCSR(g) as d:
+                    for s in (0, g.nodes // 2):
+                        dist = np.empty(g.nodes, np.int32)
+                        ig.GPUsssp_vertex(int(s), d, dist)
+                        assert np.array_equal(dist, orc.sssp(g, int(s))), (name, s, ws, wd)
+    finally:
+        for k, v in old.items():
+            ig.set_option(k, v)
+
+
+@pytest.mark.parametrize("runs,warp_list", [(1, 64), (1, 1 << 20), (0, 1 << 20), (1, 16)])
+def test_tc_short_list_expansion(ig, orc, graphs, runs, warp_list):
+    """Short probe lists expanded four consecutive slots per lane (one owner
+    search per lane and step) or one owner search per slot, alone or beside
+    the whole-warp walks: the same counts on plain and degree-ordered ids."""
+    old = {k: ig.get_option(k) for k in ("tc_runs", "tc_warp_list")}
+    try:
+        ig.set_option("tc_runs", runs)
+        ig.set_option("tc_warp_list", warp_list)
+        for name in ("rmat14", "hubby", "complete", "star", "grid64", "rmat18"):
+            for g in (graphs[name], graphs[name].degree_ordered()):
+                with ig.DeviceCSR(g) as d:
+                    assert ig.GPUtc_vertex(g.nodes, d.nindex_ptr, d.nlist_ptr)[0] == orc.tc(g), (name, runs)
+    finally:
+        for k, v in old.items():
+            ig.set_option(k, v)
