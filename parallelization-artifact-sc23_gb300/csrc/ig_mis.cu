@@ -114,14 +114,30 @@ __global__ void __launch_bounds__(kThreads) mis_persistent(MisArgs a) {
         // light vertices: sequential scan by the owning lane
         const bool light = live && (end - beg) <= 32;
         if (light) {
+          // four neighbours per step: their ids, then the statuses of the
+          // larger ones, loaded together; the first blocking one in list
+          // order decides, as in a one-by-one scan
           int outcome = kIncluded;
           int k = beg;
-          for (; k < end; k++) {
-            const int n = __ldg(&a.nlist[k]);
-            if (larger(mis_priority(n), n, pv, v)) {
-              const int s = load_status(a.status, n);
-              if (s == kIncluded) { outcome = kExcluded; break; }
-              if (s == kUndecided) { outcome = kUndecided; break; }
+          for (; k < end; k += 4) {
+            int n[4], st[4];
+            bool big[4];
+#pragma unroll
+            for (int t = 0; t < 4; t++) n[t] = k + t < end ? __ldg(&a.nlist[k + t]) : 0;
+#pragma unroll
+            for (int t = 0; t < 4; t++) {
+              big[t] = k + t < end && larger(mis_priority(n[t]), n[t], pv, v);
+              st[t] = big[t] ? load_status(a.status, n[t]) : kExcluded;
+            }
+            int stop = -1;
+#pragma unroll
+            for (int t = 3; t >= 0; t--)
+              if (st[t] != kExcluded) stop = t;
+            if (stop >= 0) {
+              const int s = stop == 0 ? st[0] : stop == 1 ? st[1] : stop == 2 ? st[2] : st[3];
+              outcome = s == kIncluded ? kExcluded : kUndecided;
+              k += stop;
+              break;
             }
           }
           if (outcome == kIncluded) {
