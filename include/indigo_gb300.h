@@ -144,15 +144,17 @@ int ig_event_elapsed_ms(void* start, void* stop, float* ms);
 /* Bound (milliseconds) on every device-side wait; default 5000. */
 int ig_set_wait_timeout_ms(int ms);
 /* Kernel tuning knobs (process-wide): blocks_per_sm, bfs_alpha (0: top-down
- * only), bfs_beta, bfs_bitmap, bfs_bu_claim, hub_degree, sssp_delta,
- * sssp_delta_scale, sssp_heavy_split, sssp_item_edges, sssp_warp_degree,
- * sssp_window_scale, sssp_window_degree, sssp_merge_below, sssp_spin_ns,
- * sssp_pair_slices, sssp_stage_flags, sssp_chunk, sssp_item_group,
- * sssp_static_pct, sssp_tail_split, sssp_claim_ahead, sssp_expanded_check,
- * mis_static_pct, pr_hub_degree, pr_chunk, pr_blocks_per_sm, pr_prefetch,
- * pr_subwarp, pr_static_pct, pr_two_pass, tc_block_chunk, tc_grab,
- * tc_warp_list, tc_runs, cc_bfs_seed, cc_rounds.  Every setting gives the same
- * results; they trade speed. */
+ * only), bfs_beta, bfs_bitmap, bfs_bu_claim, bfs_hub_degree, hub_degree,
+ * sssp_delta, sssp_delta_scale, sssp_heavy_split, sssp_item_edges,
+ * sssp_warp_degree, sssp_window_scale, sssp_window_degree, sssp_merge_below,
+ * sssp_spin_ns, sssp_pair_slices, sssp_stage_flags, sssp_chunk,
+ * sssp_item_group, sssp_static_pct, sssp_tail_split, sssp_claim_ahead,
+ * sssp_expanded_check, mis_static_pct, pr_hub_degree, pr_chunk,
+ * pr_blocks_per_sm, pr_prefetch, pr_subwarp, pr_static_pct, pr_two_pass,
+ * tc_block_chunk, tc_grab, tc_warp_list, tc_runs, cc_bfs_seed,
+ * cc_bfs_levels, cc_rounds.  Every setting gives the same results (PageRank:
+ * within its tolerance; the gather forms differ in summation order); they
+ * trade speed. */
 int ig_set_option(const char* name, long long value);
 int ig_get_option(const char* name, long long* value);
 /* Number of kernels this library has launched in the process. */

@@ -55,6 +55,10 @@ struct BfsArgs {
   // take groups of g chunks from a per-level counter, each claimed while the
   // previous group is scanned, so the level's end is even
   int bu_claim;
+  // > 0: stop after this many levels (vertices farther away stay INT_MAX);
+  // connected components use it to label only the near part of the giant
+  // component by BFS on a high-diameter graph
+  int max_level;
 };
 
 // Hot counters of the control block, slot s = level % 3: hot32(s) size of the
@@ -103,7 +107,7 @@ __global__ void __launch_bounds__(kThreads) bfs_persistent(BfsArgs a_in) {
   long long unexplored = a.edges - src_deg;
   int level = 0;
 
-  while (cur_size > 0) {
+  while (cur_size > 0 && (a.max_level <= 0 || level < a.max_level)) {
     const int slot = level % 3;
     if (gtid == 0) {
       const int ns = (level + 1) % 3;
@@ -242,14 +246,15 @@ int igk_bfs(IgExec* ex, const ig_csr* dg, int src, int* d_dist) {
   if ((rc = ig_exec_reset(ex))) return rc;
   const IgOptions& o = ig_exec_options(ex);
   BfsArgs a{dg->nindex, dg->nlist, dg->nodes, dg->edges, src, d_dist, (int*)qa, (int*)qb, (int*)hubs,
-            ex->d_ctl, ex->timeout_ns, o.hub_degree, o.bfs_alpha, o.bfs_beta, nullptr, 0,
+            ex->d_ctl, ex->timeout_ns, o.bfs_hub_degree, o.bfs_alpha, o.bfs_beta, nullptr, 0,
             o.bfs_bitmap ? (unsigned*)bits : nullptr, nullptr, o.bfs_bu_claim};
   void* args[] = {&a};
   return ig_launch_coop(ex, (const void*)bfs_persistent, kThreads, 0, o.blocks_per_sm, args, nullptr);
 }
 
-// As igk_bfs, the source read on the device from *d_src_key (see BfsArgs).
-int igk_bfs_keyed(IgExec* ex, const ig_csr* dg, const unsigned long long* d_src_key, int* d_dist) {
+// As igk_bfs, the source read on the device from *d_src_key (see BfsArgs),
+// stopping after max_level levels when max_level > 0.
+int igk_bfs_keyed(IgExec* ex, const ig_csr* dg, const unsigned long long* d_src_key, int* d_dist, int max_level) {
   const int src = 0;
   const size_t vb = (size_t)dg->nodes * sizeof(int);
   void *qa, *qb, *hubs;
@@ -262,8 +267,8 @@ int igk_bfs_keyed(IgExec* ex, const ig_csr* dg, const unsigned long long* d_src_
   if ((rc = ig_exec_reset(ex))) return rc;
   const IgOptions& o = ig_exec_options(ex);
   BfsArgs a{dg->nindex, dg->nlist, dg->nodes, dg->edges, src, d_dist, (int*)qa, (int*)qb, (int*)hubs,
-            ex->d_ctl, ex->timeout_ns, o.hub_degree, o.bfs_alpha, o.bfs_beta, nullptr, 0,
-            o.bfs_bitmap ? (unsigned*)bits : nullptr, d_src_key, o.bfs_bu_claim};
+            ex->d_ctl, ex->timeout_ns, o.bfs_hub_degree, o.bfs_alpha, o.bfs_beta, nullptr, 0,
+            o.bfs_bitmap ? (unsigned*)bits : nullptr, d_src_key, o.bfs_bu_claim, max_level};
   void* args[] = {&a};
   return ig_launch_coop(ex, (const void*)bfs_persistent, kThreads, 0, o.blocks_per_sm, args, nullptr);
 }

@@ -284,7 +284,10 @@ int igk_cc(IgExec* ex, const ig_csr* dg, int* d_label, bool sample) {
     if ((rc = ig_cuda_check((int)cudaMemsetAsync(key, 0, 64, ex->stream), "memset"))) return rc;
     cc_seed<<<grid_v, kThreads, 0, ex->stream>>>(dg->nindex, n, (unsigned long long*)key);
     ig_count_launches(1);
-    if ((rc = igk_bfs_keyed(ex, dg, (const unsigned long long*)key, d_label))) return rc;  // resets the control block
+    // at most cc_bfs_levels levels: on a high-diameter graph the BFS labels
+    // only the seed's neighbourhood and union-find links the rest
+    if ((rc = igk_bfs_keyed(ex, dg, (const unsigned long long*)key, d_label, o.cc_bfs_levels)))
+      return rc;  // resets the control block
     if ((rc = ig_scratch_get(ex->scratch, IG_SLOT_Q2, (size_t)n * sizeof(int), &hubs))) return rc;
     if ((rc = ig_cuda_check((int)cudaMemsetAsync(&ex->d_ctl->i32[1], 0x7f, sizeof(int), ex->stream), "memset")))
       return rc;

@@ -143,7 +143,7 @@ void ig_count_launches(int n);
 // Algorithm launchers (enqueue on ex->stream; errors surface in ig_exec_finish)
 // ---------------------------------------------------------------------------
 int igk_bfs(IgExec* ex, const ig_csr* dg, int src, int* d_dist);
-int igk_bfs_keyed(IgExec* ex, const ig_csr* dg, const unsigned long long* d_src_key, int* d_dist);
+int igk_bfs_keyed(IgExec* ex, const ig_csr* dg, const unsigned long long* d_src_key, int* d_dist, int max_level);
 int igk_bfs_launch_prealloc(IgExec* ex, const ig_csr* dg, int src, int* d_dist, int* qa, int* qb, int* hubs);
 int igk_sssp(IgExec* ex, const ig_csr* dg, int src, int* d_dist);
 // sample: link the first neighbours and skip the largest component's vertices

@@ -8,6 +8,7 @@ struct IgOptions {
   int bfs_bitmap;         // 1: bottom-up levels test level bitmaps instead of neighbour distances
   int bfs_bu_claim;       // bottom-up levels: 32-vertex chunks per group claimed from a counter (0: grid stride)
   int hub_degree;         // degree above which a vertex is expanded by the whole grid
+  int bfs_hub_degree;     // the same for the single-source BFS (and the connected-components seed BFS)
   long long sssp_delta;   // near/far bucket width (0 = derived from sampled weights)
   int sssp_delta_scale;   // derived width = mean weight * scale / mean degree
   int sssp_heavy_split;   // 1: heavy edges (w >= delta) relaxed once per bucket
@@ -49,6 +50,8 @@ struct IgOptions {
   int cc_bfs_seed;        // CC: 1 = the largest-degree vertex's component labelled by a BFS from it,
                           // union-find for the rest (0 = neighbour sampling, then union-find;
                           // cc_rounds chooses the sampling form)
+  int cc_bfs_levels;      // CC: the seed BFS stops after this many levels (0: runs to the end); vertices
+                          // beyond are linked by union-find
   int cc_rounds;          // CC: 1 = sampled neighbours linked one round at a time (read-only root
                           // searches, a compression after each), 0 = both in one pass with path
                           // halving, 2 = as 0 after flattening the initial forest

@@ -656,6 +656,7 @@ IgOptions& ig_options() {
       /*bfs_bitmap=*/1,
       /*bfs_bu_claim=*/0,
       /*hub_degree=*/256,
+      /*bfs_hub_degree=*/32,
       /*sssp_delta=*/0,
       /*sssp_delta_scale=*/128,
       /*sssp_heavy_split=*/0,
@@ -677,8 +678,8 @@ IgOptions& ig_options() {
       /*pr_hub_degree=*/1024,
       /*pr_chunk=*/4096,
       /*pr_blocks_per_sm=*/4,
-      /*pr_prefetch=*/1,
-      /*pr_subwarp=*/0,
+      /*pr_prefetch=*/0,
+      /*pr_subwarp=*/1,
       /*pr_static_pct=*/0,
       /*pr_two_pass=*/0,
       /*tc_block_chunk=*/4096,
@@ -686,6 +687,7 @@ IgOptions& ig_options() {
       /*tc_warp_list=*/64,
       /*tc_runs=*/0,
       /*cc_bfs_seed=*/1,
+      /*cc_bfs_levels=*/8,
       /*cc_rounds=*/0,
   };
   return o;
@@ -702,13 +704,13 @@ struct OptField {
    [](const IgOptions& o) { return (long long)o.field; }}
 static const OptField g_opt_fields[] = {
     IG_OPT(blocks_per_sm, 0, 32),     IG_OPT(bfs_alpha, 0, 1000000),   IG_OPT(bfs_beta, 1, 1000000), IG_OPT(bfs_bitmap, 0, 1), IG_OPT(bfs_bu_claim, 0, 64),
-    IG_OPT(hub_degree, 32, INT_MAX),  IG_OPT(sssp_delta, 0, INT_MAX),  IG_OPT(sssp_delta_scale, 1, 1 << 20),
+    IG_OPT(hub_degree, 32, INT_MAX), IG_OPT(bfs_hub_degree, 32, INT_MAX),  IG_OPT(sssp_delta, 0, INT_MAX),  IG_OPT(sssp_delta_scale, 1, 1 << 20),
     IG_OPT(sssp_heavy_split, 0, 1),   IG_OPT(sssp_item_edges, 32, 4096), IG_OPT(sssp_warp_degree, 1, INT_MAX),
     IG_OPT(sssp_window_scale, 0, 1 << 20), IG_OPT(sssp_window_degree, 0, INT_MAX),
     IG_OPT(sssp_merge_below, 0, INT_MAX),   IG_OPT(sssp_spin_ns, 0, 100000), IG_OPT(sssp_pair_slices, 0, 2),
     IG_OPT(sssp_stage_flags, 0, 1), IG_OPT(sssp_chunk, 1, 32), IG_OPT(sssp_item_group, 1, 32), IG_OPT(sssp_static_pct, 0, 100), IG_OPT(sssp_tail_split, 1, 32), IG_OPT(sssp_claim_ahead, 0, 1), IG_OPT(sssp_expanded_check, 0, 1), IG_OPT(mis_static_pct, 0, 100),
     IG_OPT(pr_hub_degree, 32, INT_MAX), IG_OPT(pr_chunk, 32, 1 << 24),
-    IG_OPT(pr_blocks_per_sm, 0, 32), IG_OPT(pr_prefetch, 0, 1), IG_OPT(pr_subwarp, 0, 1), IG_OPT(pr_two_pass, 0, 1), IG_OPT(pr_static_pct, 0, 100), IG_OPT(tc_block_chunk, 256, 1 << 16), IG_OPT(tc_grab, 0, 64), IG_OPT(tc_warp_list, 1, 1 << 20), IG_OPT(tc_runs, 0, 1), IG_OPT(cc_bfs_seed, 0, 1), IG_OPT(cc_rounds, 0, 2),
+    IG_OPT(pr_blocks_per_sm, 0, 32), IG_OPT(pr_prefetch, 0, 1), IG_OPT(pr_subwarp, 0, 1), IG_OPT(pr_two_pass, 0, 1), IG_OPT(pr_static_pct, 0, 100), IG_OPT(tc_block_chunk, 256, 1 << 16), IG_OPT(tc_grab, 0, 64), IG_OPT(tc_warp_list, 1, 1 << 20), IG_OPT(tc_runs, 0, 1), IG_OPT(cc_bfs_seed, 0, 1), IG_OPT(cc_bfs_levels, 0, 1 << 20), IG_OPT(cc_rounds, 0, 2),
 };
 
 int ig_options_set(IgOptions& o, const char* name, long long value) {

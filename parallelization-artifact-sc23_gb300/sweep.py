@@ -40,10 +40,10 @@ BIG = 1 << 30
 #        worklist levels, topology-driven bottom-up levels), Push = top-down
 #        only (Data), Pull = bottom-up as soon as the frontier has edges,
 #        back to top-down only for the small last levels (Topo);
-#        granularity: lists expanded by the warp's lanes, with lists above the
-#        hub degree spread over the whole grid (WarpGrid), warp only, or
-#        grid-wide for every list above 32 (Grid); Bitmap / Dist: how a pull
-#        level tests a neighbour.
+#        granularity: lists expanded by the warp's lanes, every list above
+#        32 spread over the whole grid (Grid, the default), only lists above
+#        256 (WarpGrid), or warp only; Bitmap / Dist: how a pull level tests
+#        a neighbour.
 #   SSSP parallel: V = each vertex's list expanded by the warp that holds it,
 #        E = every list cut into edge work items, VE = lists above 64 edges as
 #        work items (default); order: Window = long lists expanded near
@@ -64,10 +64,10 @@ BIG = 1 << 30
 #        groups from a counter, Static75 = 75% dealt round-robin.
 #   PR   gather: OnePass = contributions gathered while summing, TwoPass =
 #        every edge's contribution gathered first in one dense pass (measured
-#        slower: the gathers cost the same either way); granularity: WarpPair
-#        = medium lists by the whole warp two at a time, SubWarp = four at a
-#        time by 8-lane sub-warps; hub chunks of 1024 /
-#        4096 / 256 edges; Prefetch / NoPrefetch of each warp's next lists.
+#        slower: the gathers cost the same either way); granularity: SubWarp
+#        = medium lists four at a time by 8-lane sub-warps, WarpPair = by the
+#        whole warp two at a time; hub chunks of 1024 / 4096 / 256 edges;
+#        NoPrefetch / Prefetch of each warp's next lists into L2.
 #        (Pull only: push PageRank needs float atomics, not deterministic.)
 #   TC   block work items of 4096 / 1024 in-neighbours, taken by blocks in
 #        runs of 2 or 4 from a counter or dealt in a grid stride; walk: probe
@@ -75,7 +75,7 @@ BIG = 1 << 30
 #        warp, or every list through the owner search (Owner).
 STYLES = {
     "bfs": {"direction": {"PushPull": {}, "Push": {"bfs_alpha": 0}, "Pull": {"bfs_alpha": 1000000}},
-            "granularity": {"WarpGrid": {}, "Warp": {"hub_degree": BIG}, "Grid": {"hub_degree": 32}},
+            "granularity": {"Grid": {}, "WarpGrid": {"bfs_hub_degree": 256}, "Warp": {"bfs_hub_degree": BIG}},
             "test": {"Bitmap": {}, "Dist": {"bfs_bitmap": 0}}},
     "sssp": {"parallel": {"VE": {}, "V": {"sssp_warp_degree": BIG}, "E": {"sssp_warp_degree": 1}},
              "order": {"Window": {}, "NoWindow": {"sssp_window_scale": 0}},
@@ -89,9 +89,9 @@ STYLES = {
     "mis": {"residency": {"B4": {}, "B2": {"blocks_per_sm": 2}, "B8": {"blocks_per_sm": 8}},
             "schedule": {"Dynamic": {}, "Static75": {"mis_static_pct": 75}}},
     "pr": {"gather": {"OnePass": {}, "TwoPass": {"pr_two_pass": 1}},
-           "granularity": {"WarpPair": {}, "SubWarp": {"pr_subwarp": 1}},
+           "granularity": {"SubWarp": {}, "WarpPair": {"pr_subwarp": 0}},
            "hubs": {"Chunk1024": {}, "Chunk4096": {"pr_hub_degree": 4096}, "Chunk256": {"pr_hub_degree": 256}},
-           "prefetch": {"Prefetch": {}, "NoPrefetch": {"pr_prefetch": 0}}},
+           "prefetch": {"NoPrefetch": {}, "Prefetch": {"pr_prefetch": 1}}},
     "tc": {"items": {"Item4096": {}, "Item1024": {"tc_block_chunk": 1024}},
            "schedule": {"Runs2": {}, "Stride": {"tc_grab": 0}, "Runs4": {"tc_grab": 4}},
            "walk": {"Walk64": {}, "Walk96": {"tc_warp_list": 96}, "Owner": {"tc_warp_list": 1 << 20}}},

@@ -62,7 +62,8 @@ def test_kernel_option_defaults_and_ranges(ig):
                 "sssp_chunk": 32, "sssp_item_group": 8, "sssp_tail_split": 1, "sssp_claim_ahead": 0,
                 "sssp_expanded_check": 0,
                 "mis_static_pct": 0, "pr_blocks_per_sm": 4, "pr_static_pct": 0, "tc_block_chunk": 4096,
-                "tc_grab": 2, "tc_warp_list": 64, "bfs_bu_claim": 0, "cc_bfs_seed": 1}
+                "tc_grab": 2, "tc_warp_list": 64, "bfs_bu_claim": 0, "cc_bfs_seed": 1, "cc_bfs_levels": 8,
+                "bfs_hub_degree": 32, "hub_degree": 256, "pr_subwarp": 1, "pr_prefetch": 0}
     for name, value in defaults.items():
         assert ig.get_option(name) == value, name
     for name, ok, bad in [("sssp_item_edges", 4096, 4097), ("sssp_item_edges", 32, 31),

@@ -641,3 +641,22 @@ def test_tc_short_list_expansion(ig, orc, graphs, runs, warp_list):
     finally:
         for k, v in old.items():
             ig.set_option(k, v)
+
+
+@pytest.mark.parametrize("levels", [1, 2, 5, 32, 0])
+def test_cc_truncated_seed_bfs(ig, orc, graphs, levels):
+    """The seed BFS of connected components stopped after 1 / 2 / 5 / 32
+    levels or run to the end: the vertices beyond it are linked by
+    union-find and the min-id labels are exact (high-diameter grids and road
+    graphs, skewed graphs, several components)."""
+    old = ig.get_option("cc_bfs_levels")
+    try:
+        ig.set_option("cc_bfs_levels", levels)
+        for name in ("road128", "grid64", "two_grids", "rmat14", "hubby", "star", "path", "two_isolated", "rmat18"):
+            g = graphs[name]
+            lab = np.empty(g.nodes, np.int32)
+            with ig.DeviceCSR(g) as d:
+                ig.GPUcc_vertex(d, lab)
+            assert np.array_equal(lab, orc.cc(g)), (name, levels)
+    finally:
+        ig.set_option("cc_bfs_levels", old)
