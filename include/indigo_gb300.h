@@ -105,6 +105,9 @@ uint64_t ig_csr_digest(const ig_csr* g);
 int ig_device_count(int* n);
 int ig_set_device(int device);
 int ig_device_name(char* buf, int len);
+/* Free and total device memory of the current device, in bytes
+ * (cudaMemGetInfo). */
+int ig_device_memory(unsigned long long* free_bytes, unsigned long long* total_bytes);
 int ig_dev_alloc(void** ptr, size_t bytes);
 int ig_dev_free(void* ptr);
 int ig_host_alloc_pinned(void** ptr, size_t bytes);
@@ -228,9 +231,10 @@ int ig_tc_edge(long long* count, int edges, const int* d_nindex, const int* d_nl
  * (12 MiB per GPU, held until exit), so graphs are limited to 1,048,576
  * vertices (IG_ERR_INVALID_ARG beyond).  Runs on `stream` (NULL: legacy
  * default), reads back a status word and synchronizes `stream` before it
- * returns.  No cudaMalloc or cudaFree is made.  The first call on a device
- * resolves the array's address with cudaGetSymbolAddress: make it before any
- * stream capture.  That address is kept for the process's life, so after
+ * returns, so it must never be called on a stream that is being captured.
+ * No cudaMalloc or cudaFree is made.  The first call on a device resolves
+ * the array's address with cudaGetSymbolAddress.  That address is kept for
+ * the process's life, so after
  * cudaDeviceReset the entry point must not be called on that device again.
  * Calls share the array, so calls whose GPU work overlaps race; order them.
  * Errors are reported as by ig_bfs_vertex, whose results it reproduces. */

@@ -21,13 +21,14 @@
 //   * calls whose GPU work overlaps (two host threads, two streams) race on the
 //     array: the caller must order them;
 //   * the first call on each device looks up the array's device address with
-//     cudaGetSymbolAddress (once per device, that device current); make that
-//     first call before any stream capture.  The address is kept for the
-//     life of the process: after cudaDeviceReset the library's device image
-//     is loaded again and the kept address is no longer valid, so a process
-//     that resets a device must not call this entry point on it afterwards;
+//     cudaGetSymbolAddress (once per device, that device current).  The
+//     address is kept for the life of the process: after cudaDeviceReset the
+//     library's device image is loaded again and the kept address is no
+//     longer valid, so a process that resets a device must not call this
+//     entry point on it afterwards;
 //   * every call copies the device's status word back and synchronizes
-//     `stream` before it returns.
+//     `stream` before it returns, so no call may be made on a stream that is
+//     being captured.
 #include "ig_device.cuh"
 
 namespace {

@@ -200,6 +200,14 @@ extern "C" int ig_set_device(int device) {
   IG_CU(cudaSetDevice(device));
   return IG_OK;
 }
+extern "C" int ig_device_memory(unsigned long long* free_bytes, unsigned long long* total_bytes) {
+  if (!free_bytes || !total_bytes) return ig_fail(IG_ERR_INVALID_ARG, "null");
+  size_t f = 0, t = 0;
+  IG_CU(cudaMemGetInfo(&f, &t));
+  *free_bytes = f;
+  *total_bytes = t;
+  return IG_OK;
+}
 extern "C" int ig_device_name(char* buf, int len) {
   if (!buf || len < 1) return ig_fail(IG_ERR_INVALID_ARG, "null");
   int dev = 0;

@@ -100,6 +100,7 @@ SIGNATURES = {
     "ig_device_count": (_I, [_PI]),
     "ig_set_device": (_I, [_I]),
     "ig_device_name": (_I, [ctypes.c_char_p, _I]),
+    "ig_device_memory": (_I, [ctypes.POINTER(ctypes.c_ulonglong), ctypes.POINTER(ctypes.c_ulonglong)]),
     "ig_dev_alloc": (_I, [ctypes.POINTER(_P), ctypes.c_size_t]),
     "ig_dev_free": (_I, [_P]),
     "ig_host_alloc_pinned": (_I, [ctypes.POINTER(_P), ctypes.c_size_t]),
