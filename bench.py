@@ -494,8 +494,8 @@ def load_peaks() -> dict:
 # included), bfs_persistent, mis_persistent, and every kernel of the CC call
 # (its seed, its BFS and the union-find kernels).  The capture and its
 # figures are in the per-kernel traffic summary under profiles/.
-DRAM_BYTES_PER_CALL = {"sssp": 2504386466, "pr": 9044022181, "tc": 4027192374, "bfs": 155065402,
-                       "mis": 178654042, "cc": 229072574}
+DRAM_BYTES_PER_CALL = {"sssp": 2293121924, "pr": 8985803654, "tc": 4045317244, "bfs": 154965131,
+                       "mis": 179344572, "cc": 228995045}
 
 
 # ----------------------------------------------------------------------------- CPU
