@@ -10,12 +10,16 @@
 // Output semantics follow include/sssp_vertex_cuda.h: shortest distance,
 // INT_MAX if unreachable (checked there against CPUserialDijkstra, :74-99).
 //
-// Near phase: the near queue is expanded in chunks of 32 vertices per warp;
-// a vertex with more than warp_degree neighbours instead becomes work items of
-// item_edges edges, expanded in 128-edge slices, one whole warp per slice,
-// taken dynamically by the warps that have finished their frontier chunks
-// while the others still add items, so no warp holds the round up with a
-// long list and one grid barrier ends each round.  An
+// Near phase: the near queue is expanded in chunks of 32 vertices per warp
+// (the first static_pct percent of a round's chunks dealt round-robin, the
+// rest taken from a per-round counter); a vertex with more than warp_degree
+// neighbours instead becomes work items of item_edges edges, expanded after
+// the round's grid barrier in 128-edge slices, one whole warp per slice, in
+// groups dealt the same way, so no warp holds the round up with a long list
+// (with merge_below, a round with a small frontier has its first items taken
+// by the warps that have finished their chunks, one barrier per round).
+// Improved vertices are staged per warp and their queue flags settled 32 at
+// a time (stage_flags).  An
 // improved vertex with distance < T joins the next near queue
 // (once per iteration, by stamp) and otherwise the far pile (once per epoch,
 // by flag).  With expanded_check, a queued vertex is expanded only if its
