@@ -21,15 +21,15 @@
 // batched run stops each graph on its own FP64 residual.)
 //
 // Work split: groups of 32 consecutive vertices, the first static_pct
-// percent of them dealt round-robin to the warps and the rest taken one at
-// a time from a per-iteration counter (claimed one group ahead, so the
-// claim's round trip and the next group's list loads overlap the current
-// group's sums); a list's cost varies with its degree, so the counter
-// evens out the end of the iteration.  A vertex
-// with <= kLight neighbours is summed by its own lane, one with more by the
-// whole warp; a vertex above the hub degree is cut into fixed chunks of edges
-// spread over all warps, and its chunk sums are combined in chunk order after
-// a grid barrier.
+// percent of them dealt round-robin to the warps and the rest taken from a
+// per-iteration counter, a group (or a unit of groups on a graph with many)
+// per claim, claimed one ahead, so the claim's round trip and the next
+// group's list loads overlap the current group's sums; a list's cost varies
+// with its degree, so the counter evens out the end of the iteration.  A
+// vertex with <= kLight neighbours is summed by its own lane, one with more
+// by an 8-lane sub-warp (subwarp) or the whole warp; a vertex above the hub
+// degree is cut into fixed chunks of edges spread over all warps, and its
+// chunk sums are combined in chunk order after a grid barrier.
 #include <type_traits>
 
 #include "ig_device.cuh"
