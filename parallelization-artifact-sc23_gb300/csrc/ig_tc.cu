@@ -15,16 +15,19 @@
 //   3. count  : work item = (middle vertex v, a chunk of its in-neighbours
 //               u).  N+(v) is hashed into shared memory (a 2048-slot table
 //               and an 8192-bit filter shared by a whole block when N+(v)
-//               has more than 64 entries, a 128-slot table per warp
-//               otherwise) and every w of the out-lists N+(u) is probed
-//               (load-balanced warp expansion, four probes per lane in
-//               flight); a hit is the triangle u -> v -> w, counted once (at
-//               its middle vertex).  When the ids are in (degree, id) order
-//               every w of N+(v) is above v, and a middle vertex with a long
-//               N+(v) sits near the top of the id range: if fewer than 2^17
-//               ids lie above v, N+(v) is an exact bitmap over (v, V) in the
-//               block's shared memory instead (one bit test per probe, no
-//               filter and no hash walk).  Work: sum over u of |N+(u)|^2 probes,
+//               has more than 64 entries -- more than 128 when no exact
+//               bitmap applies --, a 256-slot table per warp otherwise) and
+//               every w of the out-lists N+(u) is probed (a list of at least
+//               tc_warp_list probes walked by the whole warp 128 at a time,
+//               shorter ones through a load-balanced warp expansion, four
+//               probes per lane in flight); a hit is the triangle u -> v ->
+//               w, counted once (at its middle vertex).  When the ids are in
+//               (degree, id) order every w of N+(v) is above v, and a middle
+//               vertex with a long N+(v) sits near the top of the id range:
+//               if its bitmap from v + 1's 32-id word up to id V - 1 fits 2^17
+//               bits, N+(v) is an exact bitmap in the block's shared memory
+//               instead (one shared load and bit test per probe, no filter
+//               and no hash walk).  Work: sum over u of |N+(u)|^2 probes,
 //               halved when the ids are already in (degree, id) order (the
 //               degree-ordered input of the benchmark): then only the part
 //               of N+(u) after v is scanned.  The filter rejects most misses
