@@ -29,6 +29,16 @@ def test_first_variant_is_the_default(ig):
                 ig.set_option(name, old)
 
 
+def test_every_other_word_leaves_the_default(ig):
+    """Each word after an axis's first sets at least one option to a value
+    other than the library default, so no variant repeats the default under
+    another name (it would when a default moves and the axis does not)."""
+    for algo, axes in sweep.STYLES.items():
+        for axis, words in axes.items():
+            for word, opts in list(words.items())[1:]:
+                assert any(ig.get_option(k) != v for k, v in opts.items()), (algo, axis, word)
+
+
 def test_style_words_name_the_axes():
     names = [sweep.variant_name("rmat20", a, w) for a in sweep.STYLES for w, _ in sweep.variants(a)]
     assert len(names) == len(set(names))
