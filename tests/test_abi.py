@@ -98,3 +98,22 @@ def test_dropins_reject_bad_arguments_without_device(ig):
     assert L.ig_sssp_vertex(0, ctypes.byref(hc), out.ctypes.data, ctypes.byref(t)) == ig._lib.IG_ERR_INVALID_ARG
     assert L.ig_pr(None, out.ctypes.data, None, 1e-4, 100, None, None) == ig._lib.IG_ERR_INVALID_ARG
     assert L.ig_tc_vertex(None, 4, None, None, None) == ig._lib.IG_ERR_INVALID_ARG
+
+
+def test_every_option_is_documented_and_settable(ig):
+    """Every field of the options struct (csrc/ig_options.h) is accepted by
+    ig_get_option with the default the integration table states, and is
+    named in the header's option list."""
+    import re
+    from pathlib import Path
+    root = Path(__file__).resolve().parents[1]
+    fields = re.findall(r"^\s*(?:int|long long)\s+(\w+);", (root / "parallelization-artifact-sc23_gb300" / "csrc" /
+                                                           "ig_options.h").read_text(), re.M)
+    assert len(fields) > 30
+    header = (root / "include" / "indigo_gb300.h").read_text()
+    knobs = header[header.index("Kernel tuning knobs"):header.index("int ig_set_option")]
+    table = dict(re.findall(r"^\| `(\w+)` \| (-?\d+) \|", (root / "INTEGRATION.md").read_text(), re.M))
+    for name in fields:
+        assert re.search(r"\b%s\b" % name, knobs), name
+        assert name in table, name
+        assert ig.get_option(name) == int(table[name]), name
